@@ -1,0 +1,187 @@
+/*
+ * eh_gb300.h — C ABI of the GB300 set-intersection pattern engine.
+ *
+ * Plain pointers and sizes only; no C++ or torch types cross this boundary.
+ * Every function returns an eh_status; on failure a message is available from
+ * eh_last_error() (thread-local).  Handles are opaque; the library owns the
+ * device memory behind them.  A handle may be used from one host thread at a
+ * time.  `stream` arguments are cudaStream_t values passed as void* (NULL = the
+ * legacy default stream).
+ *
+ * Each entry point names the reference interface it replaces
+ * (chrisaberger/SIMDGraphProcessing, paths relative to that project).
+ */
+#ifndef EH_GB300_H
+#define EH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum eh_status {
+  EH_OK = 0,
+  EH_ERR_INVALID_ARGUMENT = 1, /* bad handle, size, layout, unsorted row, ... */
+  EH_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+  EH_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed */
+  EH_ERR_UNSUPPORTED = 4,      /* layout / pattern combination not provided */
+  EH_ERR_IO = 5,               /* file could not be opened / was truncated */
+  EH_ERR_DEVICE_CHECK = 6,     /* a device-side bounds or consistency check fired */
+  EH_ERR_TIMEOUT = 7,          /* a bounded wait ran out */
+  EH_ERR_ADMISSION = 8         /* request rejected by the memory admission rule */
+} eh_status;
+
+/* Set layouts.  The numeric values of the first three equal the reference's
+ * common::type tags (src/common.hpp:171-181): BITSET=0, PSHORT=1, UINTEGER=2,
+ * HYBRID=5.  EH_LAYOUT_HYBRID3 is the optional three-tier optimizer
+ * (hybrid::compute_type, src/set/layouts/hybrid.hpp:55-63); EH_LAYOUT_HYBRID is
+ * the rule the reference actually runs (hybrid::get_type, hybrid.hpp:73-100). */
+typedef enum eh_layout {
+  EH_LAYOUT_BITSET = 0,
+  EH_LAYOUT_PSHORT = 1,
+  EH_LAYOUT_UINTEGER = 2,
+  EH_LAYOUT_HYBRID = 5,
+  EH_LAYOUT_HYBRID3 = 16
+} eh_layout;
+
+/* Edge selections the apps pass to SparseMatrix::build.  LOWER keeps nbr < node
+ * (apps/undirected_triangle_counting.cpp:20-23, apps/n_clique.cpp:23-26); ALL
+ * keeps every edge (apps/undirected_lollipop_counting.cpp:20-23,
+ * apps/similar_nodes.cpp:24-27).  MASK uses a caller-evaluated per-edge mask. */
+typedef enum eh_selection {
+  EH_SELECT_ALL = 0,
+  EH_SELECT_LOWER = 1,
+  EH_SELECT_MASK = 2
+} eh_selection;
+
+const char* eh_last_error(void);
+const char* eh_status_string(eh_status s);
+const char* eh_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* Host graph: the reference's MutableGraph (src/MutableGraph.hpp:49-93).     */
+/* Symmetric adjacency in CSR form: offsets[n+1] (u64), nbrs[offsets[n]] (u32)
+ * sorted ascending per row, ext_ids[n] (u64) the external id of each row.     */
+/* ------------------------------------------------------------------------- */
+typedef struct eh_hgraph* eh_hgraph_t;
+
+/* Copy a CSR adjacency into a new host graph (ext_ids may be NULL: identity). */
+eh_status eh_hgraph_from_csr(uint64_t n, const uint64_t* offsets, const uint32_t* nbrs,
+                             const uint64_t* ext_ids, eh_hgraph_t* out);
+/* MutableGraph::undirectedFromBinary (src/MutableGraph.hpp:316-360). */
+eh_status eh_hgraph_read_binary(const char* path, eh_hgraph_t* out);
+/* MutableGraph::writeUndirectedToBinary (src/MutableGraph.hpp:298-314). */
+eh_status eh_hgraph_write_binary(eh_hgraph_t g, const char* path);
+/* MutableGraph::undirectedFromEdgeList (src/MutableGraph.hpp:517-599): text
+ * "src dst" pairs; both directions inserted, rows sorted and deduplicated,
+ * self-loops kept (as the reference does). */
+eh_status eh_hgraph_read_edge_list(const char* path, eh_hgraph_t* out);
+/* MutableGraph::reorder_by_degree (src/MutableGraph.hpp:268-272) with the
+ * OrderNeighborhoodByDegree order (:20-32) and reassign_ids (:100-123). */
+eh_status eh_hgraph_reorder_by_degree(eh_hgraph_t g);
+/* Borrowed views of the arrays (valid until the graph is freed or reordered).
+ * num_edges = offsets[n] (directed entries, the reference's num_edges). */
+eh_status eh_hgraph_view(eh_hgraph_t g, uint64_t* n, uint64_t* num_edges,
+                         const uint64_t** offsets, const uint32_t** nbrs,
+                         const uint64_t** ext_ids, uint64_t* max_nbrhood_size);
+void eh_hgraph_free(eh_hgraph_t g);
+
+/* Seeded generators (no reference counterpart; the reference has none).
+ * All draw from a counter-based SplitMix64 stream so that the same call gives
+ * the same graph on any host.  Output: symmetric, deduplicated, self-loops
+ * removed, vertex ids as generated (call eh_hgraph_reorder_by_degree next).
+ * R-MAT keeps the first `num_edges` distinct undirected edges in draw order.
+ * ER is G(n, M): `num_edges` distinct uniform pairs.  BA attaches each new
+ * vertex to m distinct earlier vertices by degree-proportional choice.  The
+ * planted graph is an ER background plus `num_cliques` cliques whose sizes are
+ * log-uniform integers in [min_size, max_size] over random vertex subsets. */
+eh_status eh_generate_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c,
+                           uint64_t seed, eh_hgraph_t* out);
+eh_status eh_generate_er(uint64_t n, uint64_t num_edges, uint64_t seed, eh_hgraph_t* out);
+eh_status eh_generate_ba(uint64_t n, uint32_t m, uint64_t seed, eh_hgraph_t* out);
+eh_status eh_generate_planted_cliques(uint64_t n, uint64_t background_edges, uint32_t num_cliques,
+                                      uint32_t min_size, uint32_t max_size, uint64_t seed,
+                                      eh_hgraph_t* out);
+
+/* ------------------------------------------------------------------------- */
+/* Device matrix: the reference's SparseMatrix<T,R> (src/SparseMatrix.hpp).  */
+/* ------------------------------------------------------------------------- */
+typedef struct eh_matrix* eh_matrix_t;
+
+typedef struct eh_matrix_info {
+  uint64_t matrix_size;          /* rows (SparseMatrix::matrix_size)                  */
+  uint64_t cardinality;          /* selected edges (SparseMatrix::cardinality)       */
+  uint64_t row_total_bytes_used; /* bytes of all rows in the reference's flattened
+                                    format (SparseMatrix::row_total_bytes_used)       */
+  uint64_t max_nbrhood_size;     /* max full-graph row length (as the reference)    */
+  uint64_t max_row_cardinality;  /* max selected row length                          */
+  uint64_t num_uint_rows;        /* rows encoded per layout (common::num_uint etc.) */
+  uint64_t num_pshort_rows;
+  uint64_t num_bitset_rows;
+  uint64_t device_bytes;         /* device memory held by the matrix                 */
+  int32_t layout;                /* eh_layout                                        */
+  int32_t selection;             /* eh_selection                                     */
+} eh_matrix_info;
+
+/* SparseMatrix<T,R>::build -> from_symmetric_noattribute_graph
+ * (src/SparseMatrix.hpp:268-290,406-494) and pack_data (:249-266).
+ * Host pointers; the adjacency is copied to the device, then selected,
+ * layout-optimized and encoded there.  `edge_mask` (u8 per entry of nbrs) is
+ * read only for EH_SELECT_MASK and may be NULL otherwise. */
+eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* nbrs,
+                          const uint8_t* edge_mask, eh_selection sel, eh_layout layout,
+                          void* stream, eh_matrix_t* out);
+/* Same, with offsets / nbrs / edge_mask already in device memory. */
+eh_status eh_matrix_build_device(uint64_t n, const uint64_t* d_offsets, const uint32_t* d_nbrs,
+                                 const uint8_t* d_edge_mask, eh_selection sel, eh_layout layout,
+                                 void* stream, eh_matrix_t* out);
+eh_status eh_matrix_get_info(eh_matrix_t m, eh_matrix_info* info);
+/* Per-row layout tag (common::type), cardinality (row_lengths) and flattened
+ * byte count, copied to host arrays of matrix_size entries (any may be NULL). */
+eh_status eh_matrix_row_meta(eh_matrix_t m, uint8_t* types, uint32_t* cards, uint64_t* nbytes);
+/* Row `row` in the reference's flattened byte format, exactly as
+ * T::build_flattened writes it (hybrid.hpp:132-166, bitset.hpp:99-109,
+ * pshort.hpp:81-91, uinteger.hpp:56-59).  *nbytes receives the size; nothing is
+ * written if cap is too small (EH_ERR_INVALID_ARGUMENT). */
+eh_status eh_matrix_export_row(eh_matrix_t m, uint32_t row, uint8_t* buf, uint64_t cap,
+                               uint64_t* nbytes);
+/* SparseMatrix::get_max_row_id (src/SparseMatrix.hpp:133-145). */
+eh_status eh_matrix_get_max_row_id(eh_matrix_t m, uint32_t* row);
+/* Algorithmic bytes of one triangle-count pass:
+ * sum_i [8 + bytes(A_i)] + sum_{(i,j) selected} bytes(B_j), bytes = layout payload. */
+eh_status eh_matrix_triangle_bytes(eh_matrix_t m, uint64_t* bytes);
+void eh_matrix_free(eh_matrix_t m);
+
+/* ------------------------------------------------------------------------- */
+/* Pattern counts.  The synchronous forms write the count to host memory; the  */
+/* _async forms write it to device memory on `stream` without synchronizing.   */
+/* ------------------------------------------------------------------------- */
+/* undirected_triangle_counting<T,R>::run (apps/undirected_triangle_counting.cpp:27-65):
+ * sum_i sum_{j in row(i)} |row(i) ∩ row(j)|.  Matrix built with EH_SELECT_LOWER. */
+eh_status eh_count_triangles(eh_matrix_t m, uint64_t* count, void* stream);
+eh_status eh_count_triangles_async(eh_matrix_t m, uint64_t* d_count, void* stream);
+/* n_clique<T,R>::run / apply_function (apps/n_clique.cpp:30-101), k >= 3. */
+eh_status eh_count_cliques(eh_matrix_t m, uint32_t k, uint64_t* count, void* stream);
+eh_status eh_count_cliques_async(eh_matrix_t m, uint32_t k, uint64_t* d_count, void* stream);
+/* undirected_lollipop_counting<T,R>::run (apps/undirected_lollipop_counting.cpp:27-77).
+ * Matrix built with EH_SELECT_ALL. */
+eh_status eh_count_lollipops(eh_matrix_t m, uint64_t* count, void* stream);
+eh_status eh_count_lollipops_async(eh_matrix_t m, uint64_t* d_count, void* stream);
+/* similar_nodes<T,R>::run (apps/similar_nodes.cpp:29-68): rows i with
+ * |row(v*) ∩ row(i)| > threshold, v* = get_max_row_id().  EH_SELECT_ALL. */
+eh_status eh_similar_nodes(eh_matrix_t m, uint32_t threshold, uint64_t* count, void* stream);
+eh_status eh_similar_nodes_async(eh_matrix_t m, uint32_t threshold, uint64_t* d_count,
+                                 void* stream);
+/* ops::set_intersect on rows (src/set/ops/intersection.hpp, dispatcher :2067-2117):
+ * d_counts[p] = |row(d_a[p]) ∩ row(d_b[p])| for p < npairs (device arrays);
+ * a pair that names a row >= matrix_size gets 0xffffffff. */
+eh_status eh_intersect_rows(eh_matrix_t m, const uint32_t* d_a, const uint32_t* d_b,
+                            uint64_t npairs, uint32_t* d_counts, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EH_GB300_H */

@@ -1,0 +1,315 @@
+"""GB300-native set-intersection pattern engine (EmptyHeaded's hot path).
+
+Thin ctypes binding over the C ABI in include/eh_gb300.h, used by the tests and
+the benchmark.  The engine itself is libeh_gb300.so (CUDA for sm_103a + host
+C++); this module holds no compute.  Loading fails loudly when the library is
+missing: there is no fallback path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# Layout codes (the reference's common::type values, src/common.hpp:171-181).
+BITSET, PSHORT, UINTEGER, HYBRID, HYBRID3 = 0, 1, 2, 5, 16
+LAYOUTS = {"bs": BITSET, "bitset": BITSET, "pshort": PSHORT, "uint": UINTEGER,
+           "uinteger": UINTEGER, "hybrid": HYBRID, "hybrid3": HYBRID3}
+SELECT_ALL, SELECT_LOWER, SELECT_MASK = 0, 1, 2
+SELECTIONS = {"all": SELECT_ALL, "lower": SELECT_LOWER, "mask": SELECT_MASK}
+
+STATUS = {0: "EH_OK", 1: "EH_ERR_INVALID_ARGUMENT", 2: "EH_ERR_CUDA", 3: "EH_ERR_OUT_OF_MEMORY",
+          4: "EH_ERR_UNSUPPORTED", 5: "EH_ERR_IO", 6: "EH_ERR_DEVICE_CHECK", 7: "EH_ERR_TIMEOUT",
+          8: "EH_ERR_ADMISSION"}
+
+
+class EHError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class MatrixInfo(C.Structure):
+    _fields_ = [("matrix_size", C.c_uint64), ("cardinality", C.c_uint64),
+                ("row_total_bytes_used", C.c_uint64), ("max_nbrhood_size", C.c_uint64),
+                ("max_row_cardinality", C.c_uint64), ("num_uint_rows", C.c_uint64),
+                ("num_pshort_rows", C.c_uint64), ("num_bitset_rows", C.c_uint64),
+                ("device_bytes", C.c_uint64), ("layout", C.c_int32), ("selection", C.c_int32)]
+
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Loads libeh_gb300.so (building it first if absent and allowed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError("libeh_gb300.so is not built; run simdgraphprocessing_gb300.build.build()")
+        _build.build()
+    L = C.CDLL(path)
+    P, U64, U32, I = C.c_void_p, C.c_uint64, C.c_uint32, C.c_int
+    sig = {
+        "eh_last_error": (C.c_char_p, []),
+        "eh_status_string": (C.c_char_p, [I]),
+        "eh_version": (C.c_char_p, []),
+        "eh_hgraph_from_csr": (I, [U64, P, P, P, C.POINTER(P)]),
+        "eh_hgraph_read_binary": (I, [C.c_char_p, C.POINTER(P)]),
+        "eh_hgraph_write_binary": (I, [P, C.c_char_p]),
+        "eh_hgraph_read_edge_list": (I, [C.c_char_p, C.POINTER(P)]),
+        "eh_hgraph_reorder_by_degree": (I, [P]),
+        "eh_hgraph_view": (I, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(C.POINTER(U64)),
+                               C.POINTER(C.POINTER(U32)), C.POINTER(C.POINTER(U64)), C.POINTER(U64)]),
+        "eh_hgraph_free": (None, [P]),
+        "eh_generate_rmat": (I, [U32, U64, C.c_double, C.c_double, C.c_double, U64, C.POINTER(P)]),
+        "eh_generate_er": (I, [U64, U64, U64, C.POINTER(P)]),
+        "eh_generate_ba": (I, [U64, U32, U64, C.POINTER(P)]),
+        "eh_generate_planted_cliques": (I, [U64, U64, U32, U32, U32, U64, C.POINTER(P)]),
+        "eh_matrix_build": (I, [U64, P, P, P, I, I, P, C.POINTER(P)]),
+        "eh_matrix_build_device": (I, [U64, P, P, P, I, I, P, C.POINTER(P)]),
+        "eh_matrix_get_info": (I, [P, C.POINTER(MatrixInfo)]),
+        "eh_matrix_row_meta": (I, [P, P, P, P]),
+        "eh_matrix_export_row": (I, [P, U32, P, U64, C.POINTER(U64)]),
+        "eh_matrix_get_max_row_id": (I, [P, C.POINTER(U32)]),
+        "eh_matrix_triangle_bytes": (I, [P, C.POINTER(U64)]),
+        "eh_matrix_free": (None, [P]),
+        "eh_count_triangles": (I, [P, C.POINTER(U64), P]),
+        "eh_count_triangles_async": (I, [P, P, P]),
+        "eh_count_cliques": (I, [P, U32, C.POINTER(U64), P]),
+        "eh_count_cliques_async": (I, [P, U32, P, P]),
+        "eh_count_lollipops": (I, [P, C.POINTER(U64), P]),
+        "eh_count_lollipops_async": (I, [P, P, P]),
+        "eh_similar_nodes": (I, [P, U32, C.POINTER(U64), P]),
+        "eh_similar_nodes_async": (I, [P, U32, P, P]),
+        "eh_intersect_rows": (I, [P, P, P, U64, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != 0:
+        raise EHError(status, load().eh_last_error().decode(errors="replace"))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+class HostGraph:
+    """The reference's MutableGraph: symmetric adjacency in CSR form on the host."""
+
+    def __init__(self, handle):
+        self.h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            load().eh_hgraph_free(self.h)
+            self.h = None
+
+    @classmethod
+    def from_csr(cls, offsets, nbrs, ext_ids=None):
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        nbrs = np.ascontiguousarray(nbrs, np.uint32)
+        ext = None if ext_ids is None else np.ascontiguousarray(ext_ids, np.uint64)
+        h = C.c_void_p()
+        check(load().eh_hgraph_from_csr(len(offsets) - 1, _p(offsets), _p(nbrs), _p(ext), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_binary(cls, path):
+        h = C.c_void_p()
+        check(load().eh_hgraph_read_binary(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_edge_list(cls, path):
+        h = C.c_void_p()
+        check(load().eh_hgraph_read_edge_list(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def rmat(cls, scale, num_edges, seed, a=0.57, b=0.19, c=0.19):
+        h = C.c_void_p()
+        check(load().eh_generate_rmat(scale, num_edges, a, b, c, seed, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def er(cls, n, num_edges, seed):
+        h = C.c_void_p()
+        check(load().eh_generate_er(n, num_edges, seed, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def ba(cls, n, m, seed):
+        h = C.c_void_p()
+        check(load().eh_generate_ba(n, m, seed, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def planted_cliques(cls, n, background_edges, num_cliques, min_size, max_size, seed):
+        h = C.c_void_p()
+        check(load().eh_generate_planted_cliques(n, background_edges, num_cliques, min_size, max_size,
+                                                 seed, C.byref(h)))
+        return cls(h)
+
+    def reorder_by_degree(self):
+        check(load().eh_hgraph_reorder_by_degree(self.h))
+        return self
+
+    def write_binary(self, path):
+        check(load().eh_hgraph_write_binary(self.h, os.fsencode(path)))
+
+    def csr(self, copy=True):
+        """(offsets u64[n+1], nbrs u32[m], ext_ids u64[n], max_nbrhood_size)."""
+        n, m, mx = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        off, nb, ex = C.POINTER(C.c_uint64)(), C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint64)()
+        check(load().eh_hgraph_view(self.h, C.byref(n), C.byref(m), C.byref(off), C.byref(nb),
+                                    C.byref(ex), C.byref(mx)))
+        o = np.ctypeslib.as_array(off, (n.value + 1,))
+        b = np.ctypeslib.as_array(nb, (m.value,)) if m.value else np.zeros(0, np.uint32)
+        e = np.ctypeslib.as_array(ex, (n.value,)) if n.value else np.zeros(0, np.uint64)
+        if copy:
+            o, b, e = o.copy(), b.copy(), e.copy()
+        return o, b, e, mx.value
+
+
+class Matrix:
+    """The reference's SparseMatrix<T,R>, resident in device memory."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            load().eh_matrix_free(self.h)
+            self.h = None
+
+    @classmethod
+    def build(cls, offsets, nbrs, selection="lower", layout="hybrid", mask=None, stream=None):
+        """Host CSR arrays -> upload -> device select / optimize / encode."""
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        nbrs = np.ascontiguousarray(nbrs, np.uint32)
+        mask = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        h = C.c_void_p()
+        check(load().eh_matrix_build(len(offsets) - 1, _p(offsets), _p(nbrs), _p(mask),
+                                     SELECTIONS.get(selection, selection), LAYOUTS.get(layout, layout),
+                                     _stream(stream), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def build_device(cls, n, d_offsets, d_nbrs, selection="lower", layout="hybrid", d_mask=None,
+                     stream=None):
+        """Device pointers (ints) of offsets / nbrs already resident in HBM."""
+        h = C.c_void_p()
+        check(load().eh_matrix_build_device(n, C.c_void_p(d_offsets), C.c_void_p(d_nbrs),
+                                            None if d_mask is None else C.c_void_p(d_mask),
+                                            SELECTIONS.get(selection, selection),
+                                            LAYOUTS.get(layout, layout), _stream(stream), C.byref(h)))
+        return cls(h)
+
+    def info(self):
+        i = MatrixInfo()
+        check(load().eh_matrix_get_info(self.h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in MatrixInfo._fields_}
+
+    def row_meta(self):
+        n = self.info()["matrix_size"]
+        t = np.zeros(n, np.uint8)
+        c = np.zeros(n, np.uint32)
+        b = np.zeros(n, np.uint64)
+        check(load().eh_matrix_row_meta(self.h, _p(t), _p(c), _p(b)))
+        return t, c, b
+
+    def export_row(self, row):
+        nb = C.c_uint64()
+        st = load().eh_matrix_export_row(self.h, row, None, 0, C.byref(nb))
+        buf = np.zeros(max(1, nb.value), np.uint8)
+        check(load().eh_matrix_export_row(self.h, row, _p(buf), len(buf), C.byref(nb)))
+        del st
+        return bytes(buf[:nb.value])
+
+    def max_row_id(self):
+        r = C.c_uint32()
+        check(load().eh_matrix_get_max_row_id(self.h, C.byref(r)))
+        return r.value
+
+    def triangle_bytes(self):
+        b = C.c_uint64()
+        check(load().eh_matrix_triangle_bytes(self.h, C.byref(b)))
+        return b.value
+
+    def count_triangles(self, stream=None):
+        c = C.c_uint64()
+        check(load().eh_count_triangles(self.h, C.byref(c), _stream(stream)))
+        return c.value
+
+    def count_triangles_async(self, d_out, stream=None):
+        check(load().eh_count_triangles_async(self.h, C.c_void_p(d_out), _stream(stream)))
+
+    def count_cliques(self, k=4, stream=None):
+        c = C.c_uint64()
+        check(load().eh_count_cliques(self.h, k, C.byref(c), _stream(stream)))
+        return c.value
+
+    def count_cliques_async(self, k, d_out, stream=None):
+        check(load().eh_count_cliques_async(self.h, k, C.c_void_p(d_out), _stream(stream)))
+
+    def count_lollipops(self, stream=None):
+        c = C.c_uint64()
+        check(load().eh_count_lollipops(self.h, C.byref(c), _stream(stream)))
+        return c.value
+
+    def count_lollipops_async(self, d_out, stream=None):
+        check(load().eh_count_lollipops_async(self.h, C.c_void_p(d_out), _stream(stream)))
+
+    def similar_nodes(self, threshold=10, stream=None):
+        c = C.c_uint64()
+        check(load().eh_similar_nodes(self.h, threshold, C.byref(c), _stream(stream)))
+        return c.value
+
+    def similar_nodes_async(self, threshold, d_out, stream=None):
+        check(load().eh_similar_nodes_async(self.h, threshold, C.c_void_p(d_out), _stream(stream)))
+
+    def intersect_rows(self, d_a, d_b, npairs, d_counts, stream=None):
+        check(load().eh_intersect_rows(self.h, C.c_void_p(d_a), C.c_void_p(d_b), npairs,
+                                       C.c_void_p(d_counts), _stream(stream)))
+
+
+def graph(kind, seed, **kw):
+    """Seeded, degree-ordered generator graph -> HostGraph."""
+    if kind == "rmat":
+        g = HostGraph.rmat(kw["scale"], kw["edges"], seed, kw.get("a", 0.57), kw.get("b", 0.19),
+                           kw.get("c", 0.19))
+    elif kind == "er":
+        g = HostGraph.er(kw["n"], kw["edges"], seed)
+    elif kind == "ba":
+        g = HostGraph.ba(kw["n"], kw["m"], seed)
+    elif kind == "planted":
+        g = HostGraph.planted_cliques(kw["n"], kw["edges"], kw["cliques"], kw["min_size"],
+                                      kw["max_size"], seed)
+    else:
+        raise ValueError(kind)
+    return g.reorder_by_degree()

@@ -1,0 +1,474 @@
+// Device build of the encoded matrix: the reference's SparseMatrix::build ->
+// from_symmetric_noattribute_graph (src/SparseMatrix.hpp:268-290,406-494),
+// pack_data (:249-266), the layout optimizer hybrid::get_type
+// (src/set/layouts/hybrid.hpp:73-100) and the encoders T::build_flattened.
+//
+// Pass 1 (k_measure, one warp per row): validate the row (strictly ascending,
+// ids < n), apply the edge selection, and measure what the layout needs
+// (count, first, last, 16-bit partitions).  Choose the layout and payload size.
+// Pass 2: exclusive scan of payload sizes (16-byte units) -> row offsets.
+// Pass 3 (k_encode, one warp per row): write RowDesc and the payload.
+#include <cstdint>
+
+#include "eh_kernels.cuh"
+
+namespace eh {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ bool is_selected(int sel, uint32_t x, uint64_t row, const uint8_t* mask, uint64_t k) {
+  if (sel == 0) return true;
+  if (sel == 1) return x < row;
+  return mask[k] != 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, const uint64_t* __restrict__ off,
+                                                    const uint32_t* __restrict__ nbr,
+                                                    const uint8_t* __restrict__ mask, int sel,
+                                                    int layout, RowMeasure* __restrict__ meas,
+                                                    BuildTotals* __restrict__ tot,
+                                                    uint32_t* __restrict__ err) {
+  __shared__ unsigned long long s_sum[6];  // cardinality, ref_bytes, uint, pshort, bitset, units
+  __shared__ unsigned long long s_max[2];  // full degree, card
+  __shared__ uint32_t s_err;
+  if (threadIdx.x < 6) s_sum[threadIdx.x] = 0;
+  if (threadIdx.x < 2) s_max[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_err = 0;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
+  uint32_t flags = 0;
+  for (uint64_t row = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row < n; row += nw) {
+    const uint64_t b = off[row], e = off[row + 1];
+    uint32_t cnt = 0, parts = 0, first = 0xffffffffu, last = 0, carry = 0;
+    bool have_carry = false;
+    for (uint64_t base = b; base < e; base += 32) {
+      const uint64_t k = base + lane;
+      const bool valid = k < e;
+      const uint32_t x = valid ? nbr[k] : 0u;
+      if (valid) {
+        if (x >= n) flags |= ERRF_RANGE;
+        if (k > b && nbr[k - 1] >= x) flags |= ERRF_UNSORTED;
+      }
+      const bool s = valid && is_selected(sel, x, row, mask, k);
+      const uint32_t bal = __ballot_sync(FULL, s);
+      if (s) {
+        first = min(first, x);
+        last = max(last, x);
+      }
+      // Previous selected element (for counting distinct 16-bit prefixes).
+      const uint32_t lower = bal & ((1u << lane) - 1u);
+      const int src = lower ? 31 - __clz(lower) : (int)lane;
+      const uint32_t px = __shfl_sync(FULL, x, src);
+      const bool has_prev = lower != 0 || have_carry;
+      const uint32_t prev = lower ? px : carry;
+      const bool new_part = s && (!has_prev || (prev >> 16) != (x >> 16));
+      parts += __popc(__ballot_sync(FULL, new_part));
+      if (bal) {
+        carry = __shfl_sync(FULL, x, 31 - __clz(bal));
+        have_carry = true;
+      }
+      cnt += __popc(bal);
+    }
+    first = __reduce_min_sync(FULL, first);
+    last = __reduce_max_sync(FULL, last);
+    if (lane == 0) {
+      uint32_t type;
+      if (layout == TY_UINT) type = TY_UINT;
+      else if (layout == TY_BITSET) type = TY_BITSET;
+      else if (layout == TY_PSHORT) type = TY_PSHORT;
+      else {
+        type = TY_UINT;
+        if (cnt > 1 && last > first) {
+          const double density = (double)cnt / (double)(last - first);
+          if (layout == 16) {  // three-tier rule (hybrid::compute_type)
+            if (density > 1.0 / 32.0) type = TY_BITSET;
+            else if (density > 1.0 / 256.0) type = TY_PSHORT;
+          } else if (density > 1.0 / 256.0) {  // hybrid::get_type
+            type = TY_BITSET;
+          }
+        }
+      }
+      uint32_t len = 0, aux = 0;
+      uint64_t bytes = 0, ref = 0;
+      if (cnt >= (1u << 28)) flags |= ERRF_ROW_TOO_LONG;
+      if (type == TY_UINT) {
+        len = cnt;
+        bytes = 4ull * cnt;
+        ref = bytes;
+      } else if (type == TY_BITSET) {
+        if (cnt) {
+          aux = first >> 6;
+          len = (last >> 6) - aux + 1;
+          ref = 4 + 8 + 8ull * len;
+        }
+        bytes = 8ull * len;
+      } else {
+        if (cnt) {
+          aux = parts;
+          len = cnt + 2 * parts;
+          ref = 4 + 2ull * len;
+        }
+        bytes = 2ull * len;
+      }
+      const bool hybrid = (layout != TY_UINT && layout != TY_BITSET && layout != TY_PSHORT);
+      if (hybrid) ref += 8;
+      const uint32_t units = (uint32_t)((bytes + 15) / 16);
+      meas[row] = RowMeasure{cnt, aux, make_lt(type, len), units};
+      atomicAdd(&s_sum[0], (unsigned long long)cnt);
+      atomicAdd(&s_sum[1], (unsigned long long)ref);
+      if (type == TY_UINT) atomicAdd(&s_sum[2], 1ull);
+      else if (cnt && type == TY_PSHORT) atomicAdd(&s_sum[3], 1ull);
+      else if (cnt && type == TY_BITSET) atomicAdd(&s_sum[4], 1ull);
+      atomicAdd(&s_sum[5], (unsigned long long)units);
+      atomicMax(&s_max[0], (unsigned long long)(e - b));
+      atomicMax(&s_max[1], (unsigned long long)cnt);
+    }
+  }
+  flags = __reduce_or_sync(FULL, flags);
+  if (lane == 0 && flags) atomicOr(&s_err, flags);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&tot->cardinality, s_sum[0]);
+    atomicAdd(&tot->ref_bytes, s_sum[1]);
+    atomicAdd(&tot->num_uint, s_sum[2]);
+    atomicAdd(&tot->num_pshort, s_sum[3]);
+    atomicAdd(&tot->num_bitset, s_sum[4]);
+    atomicAdd(&tot->payload_units, s_sum[5]);
+    atomicMax(&tot->max_full_degree, s_max[0]);
+    atomicMax(&tot->max_card, s_max[1]);
+    if (s_err) atomicOr(err, s_err);
+  }
+}
+
+// ---- exclusive scan of u32 values (three passes: tiles, tile sums, add) ----
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr uint64_t kScanTile = (uint64_t)kScanThreads * kScanItems;
+
+struct UnitsOf {
+  const RowMeasure* m;
+  __device__ uint32_t operator()(uint64_t i) const { return m[i].units; }
+};
+struct Plain {
+  const uint32_t* a;
+  __device__ uint32_t operator()(uint64_t i) const { return a[i]; }
+};
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* excl) {
+  constexpr int NW = kScanThreads / 32;
+  __shared__ uint32_t s_warp[NW];
+  __shared__ uint32_t s_total;
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = v;
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULL, inc, d);
+    if (lane >= (uint32_t)d) inc += t;
+  }
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t w = lane < NW ? s_warp[lane] : 0u;
+    uint32_t wi = w;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(FULL, wi, d);
+      if (lane >= (uint32_t)d) wi += t;
+    }
+    if (lane < NW) s_warp[lane] = wi - w;
+    if (lane == 31) s_total = wi;
+  }
+  __syncthreads();
+  *excl = inc - v + s_warp[wid];
+  const uint32_t total = s_total;
+  __syncthreads();  // s_warp / s_total are reused by the next call
+  return total;
+}
+
+template <class In>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(In in, uint64_t n, uint32_t* out, uint32_t* tile_sums) {
+  const uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    v[k] = (base + k < n) ? in(base + k) : 0u;
+    s += v[k];
+  }
+  uint32_t excl;
+  uint32_t total = block_exclusive_scan(s, &excl);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < n) out[base + k] = excl;
+    excl += v[k];
+  }
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// One block scans all tile sums (looping with a carry), exclusive, in place.
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t* sums, uint64_t m) {
+  __shared__ uint32_t s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (uint64_t base = 0; base < m; base += kScanThreads) {
+    const uint64_t i = base + threadIdx.x;
+    const uint32_t v = i < m ? sums[i] : 0u;
+    uint32_t excl;
+    const uint32_t total = block_exclusive_scan(v, &excl);
+    const uint32_t carry = s_carry;
+    if (i < m) sums[i] = excl + carry;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry = carry + total;
+    __syncthreads();
+  }
+}
+
+__global__ void k_scan_add(uint32_t* out, uint64_t n, const uint32_t* tile_sums) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += tile_sums[i / kScanTile];
+}
+
+template <class In>
+cudaError_t exclusive_scan(In in, uint64_t n, uint32_t* out, uint32_t* tmp, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+  k_scan_tiles<In><<<(unsigned)tiles, kScanThreads, 0, st>>>(in, n, out, tmp);
+  k_scan_sums<<<1, kScanThreads, 0, st>>>(tmp, tiles);
+  k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, tmp);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(kBlock) k_encode(uint64_t n, const uint64_t* __restrict__ off,
+                                                   const uint32_t* __restrict__ nbr,
+                                                   const uint8_t* __restrict__ mask, int sel,
+                                                   const RowMeasure* __restrict__ meas,
+                                                   const uint32_t* __restrict__ off16,
+                                                   RowDesc* __restrict__ desc, uint4* __restrict__ arena) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
+  for (uint64_t row = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row < n; row += nw) {
+    const RowMeasure m = meas[row];
+    const uint32_t type = m.lt >> 30;
+    if (lane == 0) desc[row] = RowDesc{off16[row], m.card, m.aux, m.lt};
+    if (m.card == 0) continue;
+    const uint64_t b = off[row], e = off[row + 1];
+    uint4* dst = arena + off16[row];
+    if (type == TY_PSHORT) {
+      // Sequential partition writer (pshort::build, pshort.hpp:46-78): [hi][count-1][lo...].
+      if (lane == 0) {
+        uint16_t* s = reinterpret_cast<uint16_t*>(dst);
+        uint32_t w = 0, size_pos = 1, plen = 0, high = 0;
+        bool started = false;
+        for (uint64_t k = b; k < e; k++) {
+          const uint32_t x = nbr[k];
+          if (!is_selected(sel, x, row, mask, k)) continue;
+          const uint32_t hi = x >> 16, lo = x & 0xffffu;
+          if (started && hi == high) {
+            plen++;
+            s[w++] = (uint16_t)lo;
+          } else {
+            if (started) s[size_pos] = (uint16_t)plen;
+            s[w] = (uint16_t)hi;
+            s[w + 1] = 0;
+            s[w + 2] = (uint16_t)lo;
+            size_pos = w + 1;
+            w += 3;
+            plen = 0;
+            high = hi;
+            started = true;
+          }
+        }
+        s[size_pos] = (uint16_t)plen;
+      }
+      continue;
+    }
+    uint32_t k_sel = 0;
+    for (uint64_t base = b; base < e; base += 32) {
+      const uint64_t k = base + lane;
+      const bool valid = k < e;
+      const uint32_t x = valid ? nbr[k] : 0u;
+      const bool s = valid && is_selected(sel, x, row, mask, k);
+      const uint32_t bal = __ballot_sync(FULL, s);
+      if (s) {
+        if (type == TY_UINT) {
+          reinterpret_cast<uint32_t*>(dst)[k_sel + __popc(bal & ((1u << lane) - 1u))] = x;
+        } else {
+          unsigned long long* words = reinterpret_cast<unsigned long long*>(dst);
+          atomicOr(&words[(x >> 6) - m.aux], 1ull << (x & 63));
+        }
+      }
+      k_sel += __popc(bal);
+    }
+  }
+}
+
+__global__ void k_plan_hist(uint64_t n, const RowDesc* __restrict__ desc, uint32_t min_card,
+                            uint32_t* __restrict__ hist) {
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = desc[r].card;
+    if (c >= min_card) atomicAdd(&hist[65535u - min(c, 65535u)], 1u);
+  }
+}
+__global__ void k_plan_scatter(uint64_t n, const RowDesc* __restrict__ desc, uint32_t min_card,
+                               uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = desc[r].card;
+    if (c >= min_card) order[atomicAdd(&cursor[65535u - min(c, 65535u)], 1u)] = (uint32_t)r;
+  }
+}
+
+// Decodes whole rows into plain sorted u32 lists (one block per row).
+__global__ void k_decode_rows(const RowDesc* __restrict__ desc, const uint4* __restrict__ arena,
+                              const uint32_t* __restrict__ rows,
+                              const unsigned long long* __restrict__ dst_off, uint32_t* __restrict__ dst) {
+  const RowView V = load_view(desc, arena, rows[blockIdx.x]);
+  uint32_t* out = dst + dst_off[blockIdx.x];
+  if (V.type == TY_UINT) {
+    const uint32_t* a = static_cast<const uint32_t*>(V.p);
+    for (uint32_t k = threadIdx.x; k < V.card; k += blockDim.x) out[k] = a[k];
+    return;
+  }
+  if (threadIdx.x >= 32) return;  // one warp walks bitset words / pshort partitions in order
+  const uint32_t lane = threadIdx.x;
+  uint32_t pos = 0;
+  if (V.type == TY_BITSET) {
+    const unsigned long long* w = static_cast<const unsigned long long*>(V.p);
+    for (uint32_t base = 0; base < V.len; base += 32) {
+      const uint32_t k = base + lane;
+      unsigned long long x = k < V.len ? w[k] : 0ull;
+      const uint32_t c = __popcll(x);
+      uint32_t inc = c;
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(FULL, inc, d);
+        if (lane >= (uint32_t)d) inc += t;
+      }
+      uint32_t p = pos + inc - c;
+      while (x) {
+        out[p++] = 64u * (V.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
+        x &= x - 1ull;
+      }
+      pos += __shfl_sync(FULL, inc, 31);
+    }
+  } else {
+    const uint16_t* s = static_cast<const uint16_t*>(V.p);
+    uint32_t i = 0;
+    while (i < V.len) {
+      const uint32_t hb = (uint32_t)s[i] << 16, cnt = (uint32_t)s[i + 1] + 1;
+      for (uint32_t k = lane; k < cnt; k += 32) out[pos + k] = hb | s[i + 2 + k];
+      pos += cnt;
+      i += cnt + 2;
+    }
+  }
+}
+
+// Algorithmic bytes of one triangle pass: sum_i [8 + bytes(A_i)] + sum_{j in A_i} bytes(B_j).
+__global__ void __launch_bounds__(kBlock) k_triangle_bytes(uint64_t n, const RowDesc* __restrict__ desc,
+                                                           const uint4* __restrict__ arena,
+                                                           unsigned long long* __restrict__ out) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
+  unsigned long long acc = 0;
+  for (uint64_t row = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row < n; row += nw) {
+    const RowView A = load_view(desc, arena, (uint32_t)row);
+    if (lane == 0) acc += 8 + payload_bytes(A);
+    warp_for_each(A, 0xffffffffu, lane, [&](uint32_t j) { acc += payload_bytes(load_view(desc, arena, j)); });
+  }
+  acc = warp_sum_u64(acc);
+  if (lane == 0) atomicAdd(out, acc);
+}
+
+__global__ void k_max_row(uint64_t n, const RowDesc* __restrict__ desc, unsigned long long* out) {
+  unsigned long long best = 0;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+    // Largest card wins; among equals the smallest row id (SparseMatrix::get_max_row_id
+    // keeps the first strict maximum).
+    const unsigned long long key = ((unsigned long long)desc[r].card << 32) | (0xffffffffu - (uint32_t)r);
+    best = key > best ? key : best;
+  }
+  for (int d = 16; d; d >>= 1) {
+    unsigned long long o = __shfl_xor_sync(FULL, best, d);
+    best = o > best ? o : best;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, best);
+}
+
+}  // namespace
+
+static int grid_for(uint64_t items, int per_block) {
+  uint64_t g = (items + per_block - 1) / per_block;
+  if (g < 1) g = 1;
+  if (g > 152ull * 64) g = 152ull * 64;
+  return (int)g;
+}
+
+cudaError_t launch_measure(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
+                           int sel, int layout, RowMeasure* meas, BuildTotals* totals, uint32_t* err,
+                           cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_measure<<<grid_for(n, kBlock / 32), kBlock, 0, st>>>(n, off, nbr, mask, sel, layout, meas, totals, err);
+  return cudaGetLastError();
+}
+
+uint64_t scan_tmp_words(uint64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+cudaError_t launch_scan_units(uint64_t n, const RowMeasure* meas, uint32_t* off16, uint32_t* tmp,
+                              uint64_t n_tmp, cudaStream_t st) {
+  (void)n_tmp;
+  return exclusive_scan(UnitsOf{meas}, n, off16, tmp, st);
+}
+
+cudaError_t launch_encode(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
+                          int sel, const RowMeasure* meas, const uint32_t* off16, RowDesc* desc,
+                          uint4* arena, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_encode<<<grid_for(n, kBlock / 32), kBlock, 0, st>>>(n, off, nbr, mask, sel, meas, off16, desc, arena);
+  return cudaGetLastError();
+}
+
+// hist: 65536 + scan tmp words; counts[0] = rows in plan (host reads order count
+// from the scanned histogram).
+cudaError_t launch_plan(uint64_t n, const RowDesc* desc, uint32_t min_card, uint32_t* hist,
+                        uint32_t* order, uint32_t* cursor, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(hist, 0, 65536 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaSuccess;
+  k_plan_hist<<<grid_for(n, 256), 256, 0, st>>>(n, desc, min_card, hist);
+  e = exclusive_scan(Plain{hist}, 65536, cursor, hist + 65536, st);
+  if (e != cudaSuccess) return e;
+  // Keep the scanned starts (cursor is advanced by the scatter): copy them after the
+  // histogram so that the host can read bin starts.
+  e = cudaMemcpyAsync(hist, cursor, 65536 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  k_plan_scatter<<<grid_for(n, 256), 256, 0, st>>>(n, desc, min_card, cursor, order);
+  return cudaGetLastError();
+}
+
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint64_t n, uint32_t* out, uint32_t* tmp,
+                               cudaStream_t st) {
+  return exclusive_scan(Plain{in}, n, out, tmp, st);
+}
+
+cudaError_t launch_decode_rows(const RowDesc* desc, const uint4* arena, const uint32_t* rows,
+                               const unsigned long long* dst_off, uint32_t nrows, uint32_t* dst,
+                               cudaStream_t st) {
+  if (nrows == 0) return cudaSuccess;
+  k_decode_rows<<<nrows, 256, 0, st>>>(desc, arena, rows, dst_off, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_triangle_bytes(uint64_t n, const RowDesc* desc, const uint4* arena,
+                                  unsigned long long* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_triangle_bytes<<<grid_for(n, kBlock / 32), kBlock, 0, st>>>(n, desc, arena, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_row(uint64_t n, const RowDesc* desc, unsigned long long* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_max_row<<<grid_for(n, 256), 256, 0, st>>>(n, desc, out);
+  return cudaGetLastError();
+}
+
+}  // namespace eh

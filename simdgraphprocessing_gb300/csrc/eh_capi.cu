@@ -1,0 +1,508 @@
+// C ABI over the device matrix: build orchestration, lazily built work plans,
+// pattern counts, and host views of rows in the reference's flattened format.
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "eh_internal.h"
+#include "eh_kernels.cuh"
+
+namespace eh {
+
+struct Plan {
+  bool ready = false;
+  uint32_t* order = nullptr;  // rows with card >= 2, descending card
+  uint32_t n_order = 0, n_heavy = 0, n_giant = 0;
+  uint2* units = nullptr;     // heavy units (order position, part)
+  uint32_t n_units = 0;
+  uint32_t* giant_lists = nullptr;
+  unsigned long long* giant_off = nullptr;
+};
+
+struct Matrix {
+  int device = 0;
+  uint64_t n = 0;
+  int layout = 0, selection = 0;
+  RowDesc* desc = nullptr;
+  uint4* arena = nullptr;
+  uint64_t arena_units = 0;
+  BuildTotals tot{};
+  Plan plan;
+  uint32_t* counters = nullptr;
+  unsigned long long* result = nullptr;
+  int grid = 0;
+  int64_t vstar = -1;
+  uint64_t device_bytes = 0;
+};
+
+static eh_status cuda_fail(cudaError_t e, const char* what) {
+  return set_error(EH_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+#define CU(call, what)                         \
+  do {                                         \
+    cudaError_t _e = (call);                   \
+    if (_e != cudaSuccess) return eh::cuda_fail(_e, what); \
+  } while (0)
+
+static bool valid_layout(int l) { return l == 0 || l == 1 || l == 2 || l == 5 || l == 16; }
+static bool is_hybrid(int l) { return l == 5 || l == 16; }
+
+// Reference flattened byte count of a row (hybrid.hpp:132-166 and the inner
+// build_flattened of each layout).
+static uint64_t flattened_bytes(int layout, const RowDesc& d) {
+  const uint32_t type = desc_type(d), len = desc_len(d);
+  uint64_t inner;
+  if (type == TY_UINT) inner = 4ull * d.card;
+  else if (type == TY_BITSET) inner = d.card ? 4 + 8 + 8ull * len : 0;
+  else inner = d.card ? 4 + 2ull * len : 0;
+  return inner + (is_hybrid(layout) ? 8 : 0);
+}
+
+static eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask,
+                              int sel, int layout, cudaStream_t st, Matrix** out) {
+  EH_CHECK_ARG(out != nullptr, "out is NULL");
+  EH_CHECK_ARG(valid_layout(layout), "unknown layout %d", layout);
+  EH_CHECK_ARG(sel >= 0 && sel <= 2, "unknown selection %d", sel);
+  EH_CHECK_ARG(sel != EH_SELECT_MASK || d_mask != nullptr || n == 0, "EH_SELECT_MASK needs an edge mask");
+  EH_CHECK_ARG(n < (1ull << 32), "n=%llu exceeds the u32 vertex id space", (unsigned long long)n);
+  EH_CHECK_ARG(n == 0 || (d_off != nullptr), "offsets is NULL");
+  Matrix* m = new Matrix();
+  m->n = n;
+  m->layout = layout;
+  m->selection = sel;
+  cudaGetDevice(&m->device);
+  RowMeasure* meas = nullptr;
+  BuildTotals* tot = nullptr;
+  uint32_t* err = nullptr;
+  uint32_t* off16 = nullptr;
+  uint32_t* tmp = nullptr;
+  auto cleanup = [&]() {
+    cudaFreeAsync(meas, st);
+    cudaFreeAsync(tot, st);
+    cudaFreeAsync(err, st);
+    cudaFreeAsync(off16, st);
+    cudaFreeAsync(tmp, st);
+  };
+  auto fail = [&](eh_status s) {
+    cleanup();
+    cudaStreamSynchronize(st);
+    cudaFree(m->desc);
+    cudaFree(m->arena);
+    cudaFree(m->counters);
+    delete m;
+    return s;
+  };
+  cudaError_t e;
+  const uint64_t nn = n ? n : 1;
+  if ((e = cudaMallocAsync((void**)&meas, nn * sizeof(RowMeasure), st)) != cudaSuccess ||
+      (e = cudaMallocAsync((void**)&tot, sizeof(BuildTotals), st)) != cudaSuccess ||
+      (e = cudaMallocAsync((void**)&err, sizeof(uint32_t), st)) != cudaSuccess ||
+      (e = cudaMallocAsync((void**)&off16, nn * sizeof(uint32_t), st)) != cudaSuccess ||
+      (e = cudaMallocAsync((void**)&tmp, scan_tmp_words(nn) * sizeof(uint32_t), st)) != cudaSuccess)
+    return fail(e == cudaErrorMemoryAllocation ? set_error(EH_ERR_OUT_OF_MEMORY, "build scratch allocation failed")
+                                               : cuda_fail(e, "cudaMallocAsync"));
+  cudaMemsetAsync(tot, 0, sizeof(BuildTotals), st);
+  cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
+  if ((e = launch_measure(n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, st)) != cudaSuccess)
+    return fail(cuda_fail(e, "measure kernel"));
+  uint32_t herr = 0;
+  cudaMemcpyAsync(&m->tot, tot, sizeof(BuildTotals), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail(cuda_fail(e, "measure"));
+  if (herr) {
+    return fail(set_error(EH_ERR_INVALID_ARGUMENT, "adjacency rejected:%s%s%s",
+                          (herr & ERRF_UNSORTED) ? " a row is not strictly ascending;" : "",
+                          (herr & ERRF_RANGE) ? " a neighbour id is >= n;" : "",
+                          (herr & ERRF_ROW_TOO_LONG) ? " a row has >= 2^28 selected entries;" : ""));
+  }
+  if (m->tot.payload_units >= (1ull << 32))
+    return fail(set_error(EH_ERR_UNSUPPORTED, "encoded matrix exceeds 64 GiB"));
+  if ((e = launch_scan_units(n, meas, off16, tmp, scan_tmp_words(nn), st)) != cudaSuccess)
+    return fail(cuda_fail(e, "scan"));
+  m->arena_units = m->tot.payload_units;
+  if ((e = cudaMalloc((void**)&m->desc, nn * sizeof(RowDesc))) != cudaSuccess ||
+      (e = cudaMalloc((void**)&m->arena, (m->arena_units + 1) * 16)) != cudaSuccess ||
+      (e = cudaMalloc((void**)&m->counters, 64)) != cudaSuccess)
+    return fail(set_error(EH_ERR_OUT_OF_MEMORY, "matrix allocation (%llu bytes) failed: %s",
+                          (unsigned long long)((m->arena_units + 1) * 16 + nn * 16), cudaGetErrorString(e)));
+  m->result = reinterpret_cast<unsigned long long*>(m->counters + 8);
+  m->device_bytes = nn * sizeof(RowDesc) + (m->arena_units + 1) * 16 + 64;
+  cudaMemsetAsync(m->arena, 0, (m->arena_units + 1) * 16, st);
+  if ((e = launch_encode(n, d_off, d_nbr, d_mask, sel, meas, off16, m->desc, m->arena, st)) != cudaSuccess)
+    return fail(cuda_fail(e, "encode kernel"));
+  cleanup();
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
+    cudaFree(m->desc);
+    cudaFree(m->arena);
+    cudaFree(m->counters);
+    delete m;
+    return cuda_fail(e, "encode");
+  }
+  m->grid = pivot_grid(m->device);
+  *out = m;
+  return EH_OK;
+}
+
+static eh_status ensure_plan(Matrix* m, cudaStream_t st) {
+  Plan& p = m->plan;
+  if (p.ready) return EH_OK;
+  uint32_t* hist = nullptr;
+  uint32_t* cursor = nullptr;
+  const uint64_t nn = m->n ? m->n : 1;
+  CU(cudaMalloc((void**)&p.order, nn * sizeof(uint32_t)), "plan order allocation");
+  m->device_bytes += nn * sizeof(uint32_t);
+  CU(cudaMallocAsync((void**)&hist, (65536 + scan_tmp_words(65536)) * sizeof(uint32_t), st), "plan scratch");
+  CU(cudaMallocAsync((void**)&cursor, 65536 * sizeof(uint32_t), st), "plan scratch");
+  CU(launch_plan(m->n, m->desc, 2, hist, p.order, cursor, st), "plan kernels");
+  std::vector<uint32_t> starts(65536);
+  uint32_t total = 0;
+  CU(cudaMemcpyAsync(starts.data(), hist, 65536 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "plan copy");
+  CU(cudaMemcpyAsync(&total, cursor + 65535, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "plan copy");
+  CU(cudaStreamSynchronize(st), "plan");
+  p.n_order = m->n ? total : 0;
+  p.n_heavy = m->n ? starts[65535 - kLightMax] : 0;
+  p.n_giant = m->n ? starts[65535 - kCtaListCap] : 0;
+  // Heavy units.
+  uint32_t* cnt = nullptr;
+  uint32_t* start = nullptr;
+  uint32_t* tmp = nullptr;
+  const uint32_t nh = p.n_heavy ? p.n_heavy : 1;
+  CU(cudaMallocAsync((void**)&cnt, nh * sizeof(uint32_t), st), "unit scratch");
+  CU(cudaMallocAsync((void**)&start, nh * sizeof(uint32_t), st), "unit scratch");
+  CU(cudaMallocAsync((void**)&tmp, scan_tmp_words(nh) * sizeof(uint32_t), st), "unit scratch");
+  CU(launch_pivot_units(m->desc, p.order, p.n_heavy, cnt, st), "unit count");
+  p.n_units = 0;
+  if (p.n_heavy) {
+    CU(exclusive_scan_u32(cnt, p.n_heavy, start, tmp, st), "unit scan");
+    uint32_t last_start = 0, last_cnt = 0;
+    CU(cudaMemcpyAsync(&last_start, start + p.n_heavy - 1, 4, cudaMemcpyDeviceToHost, st), "unit copy");
+    CU(cudaMemcpyAsync(&last_cnt, cnt + p.n_heavy - 1, 4, cudaMemcpyDeviceToHost, st), "unit copy");
+    CU(cudaStreamSynchronize(st), "units");
+    p.n_units = last_start + last_cnt;
+  }
+  CU(cudaMalloc((void**)&p.units, (p.n_units ? p.n_units : 1) * sizeof(uint2)), "unit allocation");
+  m->device_bytes += (p.n_units ? p.n_units : 1) * sizeof(uint2);
+  CU(launch_pivot_unit_fill(cnt, start, p.n_heavy, p.units, st), "unit fill");
+  // Giant pivots that are not uint rows get a decoded list.
+  std::vector<uint32_t> grows(p.n_giant);
+  std::vector<unsigned long long> goff(p.n_giant ? p.n_giant : 1, 0);
+  uint64_t gtotal = 0;
+  std::vector<uint32_t> dec_rows;
+  std::vector<unsigned long long> dec_off;
+  if (p.n_giant) {
+    CU(cudaMemcpyAsync(grows.data(), p.order, p.n_giant * sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "giant copy");
+    CU(cudaStreamSynchronize(st), "giant");
+    for (uint32_t u = 0; u < p.n_giant; u++) {
+      RowDesc d;
+      CU(cudaMemcpy(&d, m->desc + grows[u], sizeof(RowDesc), cudaMemcpyDeviceToHost), "giant desc");
+      if (desc_type(d) != TY_UINT) {
+        goff[u] = gtotal;
+        dec_rows.push_back(grows[u]);
+        dec_off.push_back(gtotal);
+        gtotal += d.card;
+      }
+    }
+  }
+  CU(cudaMalloc((void**)&p.giant_off, goff.size() * sizeof(unsigned long long)), "giant allocation");
+  CU(cudaMalloc((void**)&p.giant_lists, (gtotal ? gtotal : 1) * sizeof(uint32_t)), "giant allocation");
+  m->device_bytes += goff.size() * 8 + (gtotal ? gtotal : 1) * 4;
+  CU(cudaMemcpyAsync(p.giant_off, goff.data(), goff.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, st),
+     "giant copy");
+  if (!dec_rows.empty()) {
+    uint32_t* d_rows = nullptr;
+    unsigned long long* d_off = nullptr;
+    CU(cudaMallocAsync((void**)&d_rows, dec_rows.size() * 4, st), "giant scratch");
+    CU(cudaMallocAsync((void**)&d_off, dec_off.size() * 8, st), "giant scratch");
+    CU(cudaMemcpyAsync(d_rows, dec_rows.data(), dec_rows.size() * 4, cudaMemcpyHostToDevice, st), "giant copy");
+    CU(cudaMemcpyAsync(d_off, dec_off.data(), dec_off.size() * 8, cudaMemcpyHostToDevice, st), "giant copy");
+    CU(launch_decode_rows(m->desc, m->arena, d_rows, d_off, (uint32_t)dec_rows.size(), p.giant_lists, st),
+       "giant decode");
+    cudaFreeAsync(d_rows, st);
+    cudaFreeAsync(d_off, st);
+  }
+  cudaFreeAsync(cnt, st);
+  cudaFreeAsync(start, st);
+  cudaFreeAsync(tmp, st);
+  cudaFreeAsync(hist, st);
+  cudaFreeAsync(cursor, st);
+  CU(cudaStreamSynchronize(st), "plan build");
+  p.ready = true;
+  return EH_OK;
+}
+
+static PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
+  PivotArgs a;
+  a.desc = m->desc;
+  a.arena = m->arena;
+  a.order = m->plan.order;
+  a.n_order = m->plan.n_order;
+  a.n_heavy = m->plan.n_heavy;
+  a.n_giant = m->plan.n_giant;
+  a.giant_lists = m->plan.giant_lists;
+  a.giant_off = m->plan.giant_off;
+  a.counters = m->counters;
+  a.out = out;
+  return a;
+}
+
+static eh_status finish_sync(Matrix* m, unsigned long long* d_res, uint64_t* count, cudaStream_t st) {
+  (void)m;
+  CU(cudaMemcpyAsync(count, d_res, sizeof(uint64_t), cudaMemcpyDeviceToHost, st), "result copy");
+  CU(cudaStreamSynchronize(st), "count");
+  return EH_OK;
+}
+
+}  // namespace eh
+
+using eh::Matrix;
+using eh::set_error;
+
+static Matrix* MX(eh_matrix_t m) { return reinterpret_cast<Matrix*>(m); }
+static cudaStream_t ST(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+#define CHECK_MATRIX(m)                                                      \
+  do {                                                                       \
+    if (!(m)) return set_error(EH_ERR_INVALID_ARGUMENT, "matrix is NULL");   \
+    cudaSetDevice(MX(m)->device);                                            \
+  } while (0)
+
+extern "C" {
+
+eh_status eh_matrix_build_device(uint64_t n, const uint64_t* d_offsets, const uint32_t* d_nbrs,
+                                 const uint8_t* d_edge_mask, eh_selection sel, eh_layout layout,
+                                 void* stream, eh_matrix_t* out) {
+  Matrix* m = nullptr;
+  eh_status s = eh::build_device(n, d_offsets, d_nbrs, d_edge_mask, (int)sel, (int)layout, ST(stream), &m);
+  if (s == EH_OK) *out = reinterpret_cast<eh_matrix_t>(m);
+  return s;
+}
+
+eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* nbrs, const uint8_t* edge_mask,
+                          eh_selection sel, eh_layout layout, void* stream, eh_matrix_t* out) {
+  EH_CHECK_ARG(out != nullptr, "out is NULL");
+  EH_CHECK_ARG(offsets != nullptr, "offsets is NULL");
+  EH_CHECK_ARG(n < (1ull << 32), "n=%llu exceeds the u32 vertex id space", (unsigned long long)n);
+  EH_CHECK_ARG(offsets[0] == 0, "offsets[0] must be 0");
+  const uint64_t m = offsets[n];
+  EH_CHECK_ARG(m == 0 || nbrs != nullptr, "nbrs is NULL");
+  EH_CHECK_ARG(sel != EH_SELECT_MASK || edge_mask != nullptr || m == 0, "EH_SELECT_MASK needs an edge mask");
+  for (uint64_t i = 0; i < n; i++)
+    EH_CHECK_ARG(offsets[i + 1] >= offsets[i], "offsets not monotone at row %llu", (unsigned long long)i);
+  cudaStream_t st = ST(stream);
+  uint64_t* d_off = nullptr;
+  uint32_t* d_nbr = nullptr;
+  uint8_t* d_mask = nullptr;
+  cudaError_t e;
+  if ((e = cudaMallocAsync((void**)&d_off, (n + 1) * 8, st)) != cudaSuccess ||
+      (e = cudaMallocAsync((void**)&d_nbr, (m ? m : 1) * 4, st)) != cudaSuccess ||
+      (sel == EH_SELECT_MASK && (e = cudaMallocAsync((void**)&d_mask, m ? m : 1, st)) != cudaSuccess)) {
+    cudaFreeAsync(d_off, st);
+    cudaFreeAsync(d_nbr, st);
+    return set_error(EH_ERR_OUT_OF_MEMORY, "input upload allocation failed: %s", cudaGetErrorString(e));
+  }
+  cudaMemcpyAsync(d_off, offsets, (n + 1) * 8, cudaMemcpyHostToDevice, st);
+  if (m) cudaMemcpyAsync(d_nbr, nbrs, m * 4, cudaMemcpyHostToDevice, st);
+  if (d_mask && m) cudaMemcpyAsync(d_mask, edge_mask, m, cudaMemcpyHostToDevice, st);
+  eh_status s = eh_matrix_build_device(n, d_off, d_nbr, d_mask, sel, layout, stream, out);
+  cudaFreeAsync(d_off, st);
+  cudaFreeAsync(d_nbr, st);
+  if (d_mask) cudaFreeAsync(d_mask, st);
+  return s;
+}
+
+eh_status eh_matrix_get_info(eh_matrix_t mh, eh_matrix_info* info) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(info, "info is NULL");
+  Matrix* m = MX(mh);
+  info->matrix_size = m->n;
+  info->cardinality = m->tot.cardinality;
+  info->row_total_bytes_used = m->tot.ref_bytes;
+  info->max_nbrhood_size = m->tot.max_full_degree;
+  info->max_row_cardinality = m->tot.max_card;
+  info->num_uint_rows = m->tot.num_uint;
+  info->num_pshort_rows = m->tot.num_pshort;
+  info->num_bitset_rows = m->tot.num_bitset;
+  info->device_bytes = m->device_bytes;
+  info->layout = m->layout;
+  info->selection = m->selection;
+  return EH_OK;
+}
+
+eh_status eh_matrix_row_meta(eh_matrix_t mh, uint8_t* types, uint32_t* cards, uint64_t* nbytes) {
+  CHECK_MATRIX(mh);
+  Matrix* m = MX(mh);
+  std::vector<eh::RowDesc> d(m->n);
+  if (m->n) CU(cudaMemcpy(d.data(), m->desc, m->n * sizeof(eh::RowDesc), cudaMemcpyDeviceToHost), "desc copy");
+  for (uint64_t i = 0; i < m->n; i++) {
+    if (types) types[i] = (uint8_t)eh::desc_type(d[i]);
+    if (cards) cards[i] = d[i].card;
+    if (nbytes) nbytes[i] = eh::flattened_bytes(m->layout, d[i]);
+  }
+  return EH_OK;
+}
+
+eh_status eh_matrix_export_row(eh_matrix_t mh, uint32_t row, uint8_t* buf, uint64_t cap, uint64_t* nbytes) {
+  CHECK_MATRIX(mh);
+  Matrix* m = MX(mh);
+  EH_CHECK_ARG(row < m->n, "row %u out of range", row);
+  EH_CHECK_ARG(nbytes, "nbytes is NULL");
+  eh::RowDesc d;
+  CU(cudaMemcpy(&d, m->desc + row, sizeof(d), cudaMemcpyDeviceToHost), "desc copy");
+  const uint64_t total = eh::flattened_bytes(m->layout, d);
+  *nbytes = total;
+  EH_CHECK_ARG(buf != nullptr && cap >= total, "buffer too small (%llu < %llu)", (unsigned long long)cap,
+               (unsigned long long)total);
+  const uint32_t type = eh::desc_type(d), len = eh::desc_len(d);
+  uint64_t payload = type == eh::TY_UINT ? 4ull * d.card : type == eh::TY_BITSET ? 8ull * len : 2ull * len;
+  std::vector<uint8_t> pl(payload);
+  if (payload) CU(cudaMemcpy(pl.data(), m->arena + d.off16, payload, cudaMemcpyDeviceToHost), "payload copy");
+  uint8_t* p = buf;
+  if (eh::is_hybrid(m->layout)) {
+    uint64_t tag = type;
+    memcpy(p, &tag, 8);
+    p += 8;
+  }
+  if (type == eh::TY_UINT) {
+    memcpy(p, pl.data(), payload);
+  } else if (d.card) {
+    uint32_t nb = (uint32_t)(type == eh::TY_BITSET ? 8 + payload : payload);
+    memcpy(p, &nb, 4);
+    p += 4;
+    if (type == eh::TY_BITSET) {
+      uint64_t first = d.aux;
+      memcpy(p, &first, 8);
+      p += 8;
+    }
+    memcpy(p, pl.data(), payload);
+  }
+  return EH_OK;
+}
+
+eh_status eh_matrix_get_max_row_id(eh_matrix_t mh, uint32_t* row) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(row, "row is NULL");
+  Matrix* m = MX(mh);
+  if (m->vstar < 0) {
+    CU(cudaMemset(m->result, 0, 8), "memset");
+    CU(eh::launch_max_row(m->n, m->desc, m->result, 0), "max row kernel");
+    unsigned long long key = 0;
+    CU(cudaMemcpy(&key, m->result, 8, cudaMemcpyDeviceToHost), "max row copy");
+    m->vstar = m->n ? (int64_t)(0xffffffffu - (uint32_t)(key & 0xffffffffu)) : 0;
+  }
+  *row = (uint32_t)m->vstar;
+  return EH_OK;
+}
+
+eh_status eh_matrix_triangle_bytes(eh_matrix_t mh, uint64_t* bytes) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(bytes, "bytes is NULL");
+  Matrix* m = MX(mh);
+  CU(cudaMemset(m->result, 0, 8), "memset");
+  CU(eh::launch_triangle_bytes(m->n, m->desc, m->arena, m->result, 0), "bytes kernel");
+  CU(cudaMemcpy(bytes, m->result, 8, cudaMemcpyDeviceToHost), "bytes copy");
+  return EH_OK;
+}
+
+void eh_matrix_free(eh_matrix_t mh) {
+  Matrix* m = MX(mh);
+  if (!m) return;
+  cudaSetDevice(m->device);
+  cudaFree(m->desc);
+  cudaFree(m->arena);
+  cudaFree(m->counters);
+  cudaFree(m->plan.order);
+  cudaFree(m->plan.units);
+  cudaFree(m->plan.giant_lists);
+  cudaFree(m->plan.giant_off);
+  delete m;
+}
+
+eh_status eh_count_triangles_async(eh_matrix_t mh, uint64_t* d_count, void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(d_count, "d_count is NULL");
+  Matrix* m = MX(mh);
+  if (m->selection != EH_SELECT_LOWER)
+    return set_error(EH_ERR_UNSUPPORTED, "triangle counting needs a matrix built with EH_SELECT_LOWER");
+  eh_status s = eh::ensure_plan(m, ST(stream));
+  if (s != EH_OK) return s;
+  eh::PivotArgs a = eh::pivot_args(m, reinterpret_cast<unsigned long long*>(d_count));
+  CU(eh::launch_triangles(a, m->plan.units, m->plan.n_units, m->grid, ST(stream)), "triangle kernel");
+  return EH_OK;
+}
+
+eh_status eh_count_triangles(eh_matrix_t mh, uint64_t* count, void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(count, "count is NULL");
+  eh_status s = eh_count_triangles_async(mh, reinterpret_cast<uint64_t*>(MX(mh)->result), stream);
+  if (s != EH_OK) return s;
+  return eh::finish_sync(MX(mh), MX(mh)->result, count, ST(stream));
+}
+
+eh_status eh_count_lollipops_async(eh_matrix_t mh, uint64_t* d_count, void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(d_count, "d_count is NULL");
+  Matrix* m = MX(mh);
+  eh_status s = eh::ensure_plan(m, ST(stream));
+  if (s != EH_OK) return s;
+  eh::PivotArgs a = eh::pivot_args(m, reinterpret_cast<unsigned long long*>(d_count));
+  CU(eh::launch_lollipops(a, m->plan.units, m->plan.n_units, m->grid, ST(stream)), "lollipop kernel");
+  return EH_OK;
+}
+
+eh_status eh_count_lollipops(eh_matrix_t mh, uint64_t* count, void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(count, "count is NULL");
+  eh_status s = eh_count_lollipops_async(mh, reinterpret_cast<uint64_t*>(MX(mh)->result), stream);
+  if (s != EH_OK) return s;
+  return eh::finish_sync(MX(mh), MX(mh)->result, count, ST(stream));
+}
+
+eh_status eh_similar_nodes_async(eh_matrix_t mh, uint32_t threshold, uint64_t* d_count, void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(d_count, "d_count is NULL");
+  Matrix* m = MX(mh);
+  uint32_t vstar = 0;
+  eh_status s = eh_matrix_get_max_row_id(mh, &vstar);
+  if (s != EH_OK) return s;
+  CU(eh::launch_similar(m->n, m->desc, m->arena, vstar, threshold, reinterpret_cast<unsigned long long*>(d_count),
+                        ST(stream)),
+     "similar_nodes kernel");
+  return EH_OK;
+}
+
+eh_status eh_similar_nodes(eh_matrix_t mh, uint32_t threshold, uint64_t* count, void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(count, "count is NULL");
+  eh_status s = eh_similar_nodes_async(mh, threshold, reinterpret_cast<uint64_t*>(MX(mh)->result), stream);
+  if (s != EH_OK) return s;
+  return eh::finish_sync(MX(mh), MX(mh)->result, count, ST(stream));
+}
+
+eh_status eh_intersect_rows(eh_matrix_t mh, const uint32_t* d_a, const uint32_t* d_b, uint64_t npairs,
+                            uint32_t* d_counts, void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(npairs == 0 || (d_a && d_b && d_counts), "NULL pair arrays");
+  Matrix* m = MX(mh);
+  CU(eh::launch_intersect_rows(m->n, m->desc, m->arena, d_a, d_b, npairs, d_counts, ST(stream)), "intersect kernel");
+  return EH_OK;
+}
+
+eh_status eh_count_cliques_async(eh_matrix_t mh, uint32_t k, uint64_t* d_count, void* stream) {
+  CHECK_MATRIX(mh);
+  (void)k;
+  (void)d_count;
+  (void)stream;
+  return set_error(EH_ERR_UNSUPPORTED, "clique counting is not built yet");
+}
+
+eh_status eh_count_cliques(eh_matrix_t mh, uint32_t k, uint64_t* count, void* stream) {
+  CHECK_MATRIX(mh);
+  (void)k;
+  (void)count;
+  (void)stream;
+  return set_error(EH_ERR_UNSUPPORTED, "clique counting is not built yet");
+}
+
+}  // extern "C"

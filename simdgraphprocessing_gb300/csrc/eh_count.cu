@@ -1,0 +1,384 @@
+// Pattern-count kernels over an encoded matrix.
+//
+// Triangles (apps/undirected_triangle_counting.cpp:27-65) sum, over every pivot
+// row i and every j in A_i = row(i), the intersection |A_i ∩ row(j)|.  Rows are
+// pruned (nbr < node), so row(j) only holds ids below j and the count for the
+// pair equals |{a in A_i : a < j} ∩ row(j)|; with A_i sorted and j = A_i[e]
+// those are exactly A_i[0..e).  Lollipops (apps/undirected_lollipop_counting.cpp:
+// 27-77) run on the full rows and count, for y = A_x[e], the z in A_x ∩ row(y)
+// with z < y -- the same bounded intersection -- each weighted by |A_x|.
+//
+// One persistent kernel does both.  Work comes in two tiers, both handed out
+// dynamically with an atomic counter (the GPU form of par_for_range's block
+// stealing, src/common.hpp:214-276):
+//  * heavy pivots (|A_i| > kLightMax) are split into units of kUnitSpan values
+//    of e; a CTA stages the pivot's decoded list (and, for bitset rows, its
+//    words) in shared memory and its warps take one j each.  Per pair the warp
+//    picks the cheapest of: AND of overlapping bitset words + popc (bitset ∩
+//    bitset, intersection.hpp:880-955); probing each A_i[t], t < e, into row(j)
+//    (uint ∩ bitset probe, :1023-1058, or the galloping search of :393-584);
+//    streaming row(j) and looking each element up in the staged pivot (merge,
+//    :696-771).
+//  * light pivots run one per warp: the pivot is decoded into the warp's slice
+//    of shared memory and all (e, t) pairs with t < e are probed at once, one
+//    pair per lane, so short rows keep every lane busy.
+// Per-lane counts stay in registers; one u64 atomic per CTA at the end replaces
+// the reference's per-thread padded t_count array.
+#include <cstdint>
+
+#include "eh_kernels.cuh"
+
+namespace eh {
+
+namespace {
+
+constexpr int NWARPS = kCtaThreads / 32;
+constexpr uint32_t kUnitSpan = 128;   // values of e per heavy unit
+constexpr uint32_t kLightChunk = 16;  // light pivots per atomic grab
+
+struct __align__(16) PivotSmem {
+  unsigned long long words[kCtaWordCap];
+  uint32_t list[kCtaListCap];
+  uint32_t wlist[NWARPS][kLightMax];
+  uint32_t scan[kCtaThreads];
+  uint32_t unit;
+};
+
+// CTA-cooperative decode of a row into a sorted u32 list in shared memory.
+__device__ void cta_decode(const RowView& A, uint32_t* list, uint32_t* scan) {
+  const uint32_t tid = threadIdx.x;
+  if (A.type == TY_UINT) {
+    const uint32_t* a = static_cast<const uint32_t*>(A.p);
+    for (uint32_t k = tid; k < A.card; k += kCtaThreads) list[k] = a[k];
+    return;
+  }
+  if (A.type == TY_BITSET) {
+    // Thread t owns words [t*W/T, (t+1)*W/T); exclusive scan of their popcounts
+    // gives each thread its output position.
+    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
+    const uint32_t W = A.len;
+    const uint32_t w0 = (uint32_t)(((uint64_t)W * tid) / kCtaThreads);
+    const uint32_t w1 = (uint32_t)(((uint64_t)W * (tid + 1)) / kCtaThreads);
+    uint32_t c = 0;
+    for (uint32_t k = w0; k < w1; k++) c += __popcll(w[k]);
+    scan[tid] = c;
+    __syncthreads();
+    // Hillis-Steele inclusive scan over kCtaThreads values.
+    for (uint32_t d = 1; d < kCtaThreads; d <<= 1) {
+      const uint32_t v = tid >= d ? scan[tid - d] : 0u;
+      __syncthreads();
+      scan[tid] += v;
+      __syncthreads();
+    }
+    uint32_t pos = scan[tid] - c;
+    for (uint32_t k = w0; k < w1; k++) {
+      unsigned long long x = w[k];
+      while (x) {
+        list[pos++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
+        x &= x - 1ull;
+      }
+    }
+    return;
+  }
+  if (tid < 32) {  // pshort: walk the partitions with one warp
+    const uint16_t* s = static_cast<const uint16_t*>(A.p);
+    uint32_t i = 0, pos = 0;
+    while (i < A.len) {
+      const uint32_t hb = (uint32_t)s[i] << 16, cnt = (uint32_t)s[i + 1] + 1;
+      for (uint32_t k = tid; k < cnt; k += 32) list[pos + k] = hb | s[i + 2 + k];
+      pos += cnt;
+      i += cnt + 2;
+    }
+  }
+}
+
+// Warp-cooperative decode into the warp's slice (card <= kLightMax).
+__device__ __forceinline__ void warp_decode(const RowView& A, uint32_t* list, uint32_t lane) {
+  if (A.type == TY_UINT) {
+    const uint32_t* a = static_cast<const uint32_t*>(A.p);
+    for (uint32_t k = lane; k < A.card; k += 32) list[k] = a[k];
+  } else if (A.type == TY_BITSET) {
+    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
+    uint32_t pos = 0;
+    for (uint32_t base = 0; base < A.len; base += 32) {
+      const uint32_t k = base + lane;
+      unsigned long long x = k < A.len ? w[k] : 0ull;
+      const uint32_t c = __popcll(x);
+      uint32_t inc = c;
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, inc, d);
+        if (lane >= (uint32_t)d) inc += t;
+      }
+      uint32_t p = pos + inc - c;
+      while (x) {
+        list[p++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
+        x &= x - 1ull;
+      }
+      pos += __shfl_sync(FULL, inc, 31);
+    }
+  } else {
+    const uint16_t* s = static_cast<const uint16_t*>(A.p);
+    uint32_t i = 0, pos = 0;
+    while (i < A.len) {
+      const uint32_t hb = (uint32_t)s[i] << 16, cnt = (uint32_t)s[i + 1] + 1;
+      for (uint32_t k = lane; k < cnt; k += 32) list[pos + k] = hb | s[i + 2 + k];
+      pos += cnt;
+      i += cnt + 2;
+    }
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ uint32_t ilog2p1(uint32_t x) { return 32u - __clz(x | 1u); }
+
+// |{t < e : L[t] in B}| with j = L[e]; warp-uniform result.  A is the pivot row
+// (shared or global payload), L its sorted elements.
+__device__ uint32_t pair_count_warp(const uint32_t* L, uint32_t e, const RowView& A, const RowView& B,
+                                    uint32_t j, uint32_t lane) {
+  if (B.card == 0 || e == 0) return 0;
+  uint32_t c = 0;
+  if (A.type == TY_BITSET && B.type == TY_BITSET) {
+    const uint32_t lo = max(A.aux, B.aux);
+    const uint32_t hi = min(min(A.aux + A.len, B.aux + B.len), (j >> 6) + 1);
+    if (hi <= lo) return 0;
+    if (hi - lo <= 2 * e) {
+      const unsigned long long* wa = static_cast<const unsigned long long*>(A.p);
+      const unsigned long long* wb = static_cast<const unsigned long long*>(B.p);
+      const unsigned long long last_mask = (1ull << (j & 63)) - 1ull;
+      for (uint32_t w = lo + lane; w < hi; w += 32) {
+        unsigned long long x = wa[w - A.aux] & wb[w - B.aux];
+        if (w == (j >> 6)) x &= last_mask;
+        c += __popcll(x);
+      }
+      return warp_sum_u32(c);
+    }
+  }
+  // Probe cost: e lookups into B.  Stream cost: |B| lookups into the pivot.
+  bool stream = false;
+  if (B.type == TY_UINT) {
+    const uint32_t look = (A.type == TY_BITSET) ? 1u : ilog2p1(e);
+    stream = (uint64_t)B.card * look < (uint64_t)e * ilog2p1(B.card) * 4u;
+  } else if (B.type == TY_PSHORT) {
+    stream = (uint64_t)B.card * ilog2p1(e) < (uint64_t)e * (B.aux + ilog2p1(B.card)) * 4u;
+  }
+  if (!stream) {
+    for (uint32_t t = lane; t < e; t += 32) c += row_contains(B, L[t]);
+  } else if (A.type == TY_BITSET) {
+    warp_for_each(B, j, lane, [&](uint32_t y) { c += row_contains(A, y); });
+  } else {
+    warp_for_each(B, j, lane, [&](uint32_t y) {
+      const uint32_t p = lower_bound_u32(L, 0, e, y);
+      c += (p < e && L[p] == y);
+    });
+  }
+  return warp_sum_u32(c);
+}
+
+template <bool LOLLI>
+__global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2* __restrict__ units,
+                                                        uint32_t n_units) {
+  __shared__ PivotSmem s;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long acc = 0;
+
+  // ---- heavy pivots: CTA-wide units ----
+  for (;;) {
+    if (threadIdx.x == 0) s.unit = atomicAdd(&a.counters[0], 1u);
+    __syncthreads();
+    const uint32_t unit = s.unit;
+    if (unit >= n_units) break;
+    const uint2 uu = units[unit];
+    const uint32_t i = a.order[uu.x];
+    RowView A = load_view(a.desc, a.arena, i);
+    const uint32_t* L;
+    if (uu.x < a.n_giant) {
+      L = (A.type == TY_UINT) ? static_cast<const uint32_t*>(A.p) : a.giant_lists + a.giant_off[uu.x];
+    } else {
+      cta_decode(A, s.list, s.scan);
+      L = s.list;
+    }
+    if (A.type == TY_BITSET && A.len <= kCtaWordCap) {
+      const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
+      for (uint32_t k = threadIdx.x; k < A.len; k += kCtaThreads) s.words[k] = w[k];
+      A.p = s.words;
+    }
+    __syncthreads();
+    const uint32_t c = A.card;
+    const uint32_t e0 = 1 + uu.y * kUnitSpan;
+    const uint32_t e1 = min(c, e0 + kUnitSpan);
+    for (uint32_t e = e0 + warp; e < e1; e += NWARPS) {
+      const uint32_t j = L[e];
+      const RowView B = load_view(a.desc, a.arena, j);
+      const uint32_t cnt = pair_count_warp(L, e, A, B, j, lane);
+      if (lane == 0) acc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+    }
+    __syncthreads();
+  }
+
+  // ---- light pivots: one warp each, all (e, t) pairs probed in parallel ----
+  const uint32_t n_light = a.n_order - a.n_heavy;
+  uint32_t* list = s.wlist[warp];
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&a.counters[1], kLightChunk);
+    base = __shfl_sync(FULL, base, 0);
+    if (base >= n_light) break;
+    const uint32_t end = min(n_light, base + kLightChunk);
+    for (uint32_t k = base; k < end; k++) {
+      const RowView A = load_view(a.desc, a.arena, a.order[a.n_heavy + k]);
+      const uint32_t c = A.card;
+      warp_decode(A, list, lane);
+      const uint32_t pairs = c * (c - 1) / 2;
+      // Lane q starts at pair q = e(e-1)/2 + t and advances by 32 pairs a step.
+      uint32_t e = 1, t = lane;
+      while (t >= e) { t -= e; e++; }
+      uint32_t cnt = 0;
+      for (uint32_t q = lane; q < pairs; q += 32) {
+        const RowView B = load_view(a.desc, a.arena, list[e]);
+        cnt += row_contains(B, list[t]);
+        t += 32;
+        while (t >= e && e < c) { t -= e; e++; }
+      }
+      acc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+      __syncwarp();
+    }
+  }
+
+  // ---- reduce: warp, CTA, one atomic ----
+  acc = warp_sum_u64(acc);
+  __shared__ unsigned long long s_red[NWARPS];
+  if (lane == 0) s_red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < NWARPS; w++) tot += s_red[w];
+    if (tot) atomicAdd(a.out, tot);
+  }
+}
+
+// Heavy units: for order position u < n_heavy, ceil((card-1)/kUnitSpan) units (u, part).
+__global__ void k_unit_counts(const RowDesc* __restrict__ desc, const uint32_t* __restrict__ order,
+                              uint32_t n_heavy, uint32_t* __restrict__ cnt) {
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u < n_heavy) {
+    const uint32_t c = desc[order[u]].card;
+    cnt[u] = (c - 1 + kUnitSpan - 1) / kUnitSpan;
+  }
+}
+__global__ void k_unit_fill(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ start,
+                            uint32_t n_heavy, uint2* __restrict__ units) {
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u < n_heavy)
+    for (uint32_t p = 0; p < cnt[u]; p++) units[start[u] + p] = make_uint2(u, p);
+}
+
+// similar_nodes: rows i with |row(v*) ∩ row(i)| > threshold; one warp per row,
+// each element of row(i) probed into row(v*).
+__global__ void __launch_bounds__(256) k_similar(uint64_t n, const RowDesc* __restrict__ desc,
+                                                 const uint4* __restrict__ arena, uint32_t vstar,
+                                                 uint32_t threshold, unsigned long long* out) {
+  const uint32_t lane = threadIdx.x & 31;
+  const RowView A = load_view(desc, arena, vstar);
+  unsigned long long acc = 0;
+  const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
+  for (uint64_t r = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < n; r += nw) {
+    const RowView B = load_view(desc, arena, (uint32_t)r);
+    uint32_t c = 0;
+    if (A.card && B.card) warp_for_each(B, 0xffffffffu, lane, [&](uint32_t y) { c += row_contains(A, y); });
+    c = warp_sum_u32(c);
+    if (lane == 0 && c > threshold) acc++;
+  }
+  if (lane == 0 && acc) atomicAdd(out, acc);
+}
+
+// counts[p] = |row(a[p]) ∩ row(b[p])|: the smaller row is streamed and probed
+// into the larger one.  A pair naming a row >= n gets 0xffffffff.
+__global__ void __launch_bounds__(256) k_intersect_rows(uint64_t n, const RowDesc* __restrict__ desc,
+                                                        const uint4* __restrict__ arena,
+                                                        const uint32_t* __restrict__ ra,
+                                                        const uint32_t* __restrict__ rb, uint64_t np,
+                                                        uint32_t* __restrict__ counts) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
+  for (uint64_t p = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); p < np; p += nw) {
+    if (ra[p] >= n || rb[p] >= n) {
+      if (lane == 0) counts[p] = 0xffffffffu;
+      continue;
+    }
+    RowView A = load_view(desc, arena, ra[p]);
+    RowView B = load_view(desc, arena, rb[p]);
+    if (A.card > B.card) {
+      const RowView T = A;
+      A = B;
+      B = T;
+    }
+    uint32_t c = 0;
+    if (A.card && B.card) warp_for_each(A, 0xffffffffu, lane, [&](uint32_t y) { c += row_contains(B, y); });
+    c = warp_sum_u32(c);
+    if (lane == 0) counts[p] = c;
+  }
+}
+
+}  // namespace
+
+int pivot_grid(int device) {
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pivots<false>, kCtaThreads, 0);
+  if (per < 1) per = 1;
+  return sms * per;
+}
+
+template <bool LOLLI>
+static cudaError_t launch_pivots(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
+                                 cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(a.counters, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(a.out, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  k_pivots<LOLLI><<<grid, kCtaThreads, 0, st>>>(a, units, n_units);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pivot_units(const RowDesc* desc, const uint32_t* order, uint32_t n_heavy,
+                               uint32_t* cnt, cudaStream_t st) {
+  if (n_heavy == 0) return cudaSuccess;
+  k_unit_counts<<<(n_heavy + 255) / 256, 256, 0, st>>>(desc, order, n_heavy, cnt);
+  return cudaGetLastError();
+}
+cudaError_t launch_pivot_unit_fill(const uint32_t* cnt, const uint32_t* start, uint32_t n_heavy,
+                                   uint2* units, cudaStream_t st) {
+  if (n_heavy == 0) return cudaSuccess;
+  k_unit_fill<<<(n_heavy + 255) / 256, 256, 0, st>>>(cnt, start, n_heavy, units);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_triangles(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
+                             cudaStream_t st) {
+  return launch_pivots<false>(a, units, n_units, grid, st);
+}
+cudaError_t launch_lollipops(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
+                             cudaStream_t st) {
+  return launch_pivots<true>(a, units, n_units, grid, st);
+}
+
+cudaError_t launch_similar(uint64_t n, const RowDesc* desc, const uint4* arena, uint32_t vstar,
+                           uint32_t threshold, unsigned long long* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess || n == 0) return e;
+  uint64_t g = (n + 7) / 8;
+  if (g > 152 * 32) g = 152 * 32;
+  k_similar<<<(unsigned)g, 256, 0, st>>>(n, desc, arena, vstar, threshold, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_intersect_rows(uint64_t n, const RowDesc* desc, const uint4* arena, const uint32_t* a,
+                                  const uint32_t* b, uint64_t np, uint32_t* counts, cudaStream_t st) {
+  if (np == 0) return cudaSuccess;
+  uint64_t g = (np + 7) / 8;
+  if (g > 152 * 32) g = 152 * 32;
+  k_intersect_rows<<<(unsigned)g, 256, 0, st>>>(n, desc, arena, a, b, np, counts);
+  return cudaGetLastError();
+}
+
+}  // namespace eh

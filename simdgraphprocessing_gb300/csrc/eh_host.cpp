@@ -1,0 +1,486 @@
+// Host side of the engine: error reporting, the host graph (the reference's
+// MutableGraph, src/MutableGraph.hpp), its binary / edge-list formats, degree
+// ordering, and the seeded graph generators.
+//
+// Compiled with -ffp-contract=off so that the few double-precision steps in the
+// generators round identically on x86-64 and aarch64 hosts.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <numeric>
+#include <parallel/algorithm>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include <omp.h>
+
+#include "eh_internal.h"
+
+namespace eh {
+
+static thread_local std::string g_last_error;
+
+eh_status set_error(eh_status s, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return s;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+void csr_from_undirected_keys(uint64_t n, std::vector<uint64_t>& keys, HostGraph& g) {
+  g.n = n;
+  g.offsets.assign(n + 1, 0);
+  std::vector<uint64_t> deg(n, 0);
+  for (uint64_t k : keys) {
+    deg[k >> 32]++;
+    deg[k & 0xffffffffu]++;
+  }
+  for (uint64_t i = 0; i < n; i++) g.offsets[i + 1] = g.offsets[i] + deg[i];
+  g.nbrs.assign(g.offsets[n], 0);
+  std::vector<uint64_t> cur(g.offsets.begin(), g.offsets.end() - 1);
+  for (uint64_t k : keys) {
+    uint32_t lo = (uint32_t)(k >> 32), hi = (uint32_t)(k & 0xffffffffu);
+    g.nbrs[cur[lo]++] = hi;
+    g.nbrs[cur[hi]++] = lo;
+  }
+  std::vector<uint64_t>().swap(keys);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t i = 0; i < (int64_t)n; i++)
+    std::sort(g.nbrs.begin() + g.offsets[i], g.nbrs.begin() + g.offsets[i + 1]);
+  uint64_t mx = 0;
+  for (uint64_t i = 0; i < n; i++) mx = std::max(mx, g.offsets[i + 1] - g.offsets[i]);
+  g.max_nbrhood_size = mx;
+  g.ext_ids.resize(n);
+  std::iota(g.ext_ids.begin(), g.ext_ids.end(), 0);
+}
+
+// ---------------------------------------------------------------------------
+// Counter-based random stream: value(k) = SplitMix64 finalizer applied to
+// key + (k+1) * golden-gamma (Steele, Lea, Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014).  Identical on every host.
+// ---------------------------------------------------------------------------
+static inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+struct Stream {
+  uint64_t key;
+  Stream(uint64_t seed, uint64_t tag) : key(mix64(seed * 0xD1B54A32D192ED03ULL + tag)) {}
+  inline uint64_t at(uint64_t ctr) const { return mix64(key + (ctr + 1) * 0x9E3779B97F4A7C15ULL); }
+};
+// Uniform integer in [0, bound) by 64x64->128 multiply-high.
+static inline uint64_t bounded(uint64_t r, uint64_t bound) {
+  return (uint64_t)(((unsigned __int128)r * bound) >> 64);
+}
+static inline uint64_t ukey(uint64_t u, uint64_t v) {
+  return u < v ? (u << 32) | v : (v << 32) | u;
+}
+static const uint64_t kSelfLoop = ~0ULL;
+
+// Keeps the first `target` distinct keys in draw order.  `draw(lo, hi, out)`
+// fills out[k - lo] for draws k in [lo, hi) (kSelfLoop for draws to discard).
+template <class Draw>
+static bool first_distinct(uint64_t target, uint64_t first_batch, Draw draw,
+                           std::vector<uint64_t>& result) {
+  struct KI {
+    uint64_t key;
+    uint64_t idx;
+  };
+  std::vector<uint64_t> draws;
+  uint64_t total = 0, batch = std::max<uint64_t>(first_batch, 1024);
+  for (int round = 0; round < 64; round++) {
+    draws.resize(total + batch);
+    draw(total, total + batch, draws.data() + total);
+    total += batch;
+    std::vector<KI> v(total);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < (int64_t)total; k++) v[k] = KI{draws[k], (uint64_t)k};
+    __gnu_parallel::sort(v.begin(), v.end(), [](const KI& a, const KI& b) {
+      return a.key < b.key || (a.key == b.key && a.idx < b.idx);
+    });
+    std::vector<KI> heads;
+    heads.reserve(total);
+    for (uint64_t k = 0; k < total; k++) {
+      if (v[k].key == kSelfLoop) break;  // kSelfLoop sorts last
+      if (k == 0 || v[k].key != v[k - 1].key) heads.push_back(v[k]);
+    }
+    if (heads.size() >= target) {
+      std::vector<uint64_t> idx(heads.size());
+      for (size_t h = 0; h < heads.size(); h++) idx[h] = heads[h].idx;
+      uint64_t cutoff = ~0ULL;
+      if (target > 0) {
+        std::nth_element(idx.begin(), idx.begin() + (target - 1), idx.end());
+        cutoff = idx[target - 1];
+      }
+      result.clear();
+      result.reserve(target);
+      if (target > 0)
+        for (const KI& h : heads)
+          if (h.idx <= cutoff) result.push_back(h.key);
+      return true;  // result is sorted by key
+    }
+    // Grow the draw count in proportion to the shortfall.
+    double yield = (double)heads.size() / (double)total;
+    uint64_t need = (uint64_t)((double)(target - heads.size()) / std::max(yield, 1e-3) * 1.2) + 1024;
+    batch = need;
+  }
+  return false;
+}
+
+static eh_status finish_graph(uint64_t n, std::vector<uint64_t>& keys, eh_hgraph_t* out) {
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  csr_from_undirected_keys(n, keys, *g);
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
+}
+
+}  // namespace eh
+
+using eh::HostGraph;
+using eh::set_error;
+
+static HostGraph* HG(eh_hgraph_t g) { return reinterpret_cast<HostGraph*>(g); }
+
+extern "C" {
+
+const char* eh_last_error(void) { return eh::g_last_error.c_str(); }
+
+const char* eh_status_string(eh_status s) {
+  switch (s) {
+    case EH_OK: return "EH_OK";
+    case EH_ERR_INVALID_ARGUMENT: return "EH_ERR_INVALID_ARGUMENT";
+    case EH_ERR_CUDA: return "EH_ERR_CUDA";
+    case EH_ERR_OUT_OF_MEMORY: return "EH_ERR_OUT_OF_MEMORY";
+    case EH_ERR_UNSUPPORTED: return "EH_ERR_UNSUPPORTED";
+    case EH_ERR_IO: return "EH_ERR_IO";
+    case EH_ERR_DEVICE_CHECK: return "EH_ERR_DEVICE_CHECK";
+    case EH_ERR_TIMEOUT: return "EH_ERR_TIMEOUT";
+    case EH_ERR_ADMISSION: return "EH_ERR_ADMISSION";
+  }
+  return "EH_ERR_UNKNOWN";
+}
+
+const char* eh_version(void) { return "eh-gb300 0.1 (sm_103a)"; }
+
+eh_status eh_hgraph_from_csr(uint64_t n, const uint64_t* offsets, const uint32_t* nbrs,
+                             const uint64_t* ext_ids, eh_hgraph_t* out) {
+  EH_CHECK_ARG(out != nullptr, "out is NULL");
+  EH_CHECK_ARG(offsets != nullptr, "offsets is NULL");
+  EH_CHECK_ARG(n < (1ULL << 32), "n=%llu exceeds the u32 vertex id space", (unsigned long long)n);
+  EH_CHECK_ARG(offsets[0] == 0, "offsets[0] must be 0");
+  for (uint64_t i = 0; i < n; i++)
+    EH_CHECK_ARG(offsets[i + 1] >= offsets[i], "offsets not monotone at row %llu",
+                 (unsigned long long)i);
+  EH_CHECK_ARG(offsets[n] == 0 || nbrs != nullptr, "nbrs is NULL");
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  g->n = n;
+  g->offsets.assign(offsets, offsets + n + 1);
+  g->nbrs.assign(nbrs, nbrs + offsets[n]);
+  g->ext_ids.resize(n);
+  uint64_t mx = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    g->ext_ids[i] = ext_ids ? ext_ids[i] : i;
+    mx = std::max(mx, offsets[i + 1] - offsets[i]);
+  }
+  g->max_nbrhood_size = mx;
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
+}
+
+eh_status eh_hgraph_read_binary(const char* path, eh_hgraph_t* out) {
+  EH_CHECK_ARG(path && out, "path/out is NULL");
+  FILE* f = fopen(path, "rb");
+  if (!f) return set_error(EH_ERR_IO, "cannot open %s", path);
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) {
+    fclose(f);
+    return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  }
+  uint64_t n = 0;
+  bool ok = fread(&n, sizeof(n), 1, f) == 1 && n < (1ULL << 32);
+  if (ok) {
+    g->n = n;
+    g->offsets.assign(n + 1, 0);
+    g->ext_ids.resize(n);
+    for (uint64_t i = 0; i < n && ok; i++) {
+      uint64_t hdr[2];
+      ok = fread(hdr, sizeof(uint64_t), 2, f) == 2;
+      if (!ok) break;
+      g->ext_ids[i] = hdr[0];
+      g->offsets[i + 1] = g->offsets[i] + hdr[1];
+      g->max_nbrhood_size = std::max(g->max_nbrhood_size, hdr[1]);
+      size_t at = g->nbrs.size();
+      g->nbrs.resize(at + hdr[1]);
+      if (hdr[1]) ok = fread(g->nbrs.data() + at, sizeof(uint32_t), hdr[1], f) == hdr[1];
+    }
+  }
+  fclose(f);
+  if (!ok) {
+    delete g;
+    return set_error(EH_ERR_IO, "truncated or malformed binary graph %s", path);
+  }
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
+}
+
+eh_status eh_hgraph_write_binary(eh_hgraph_t gh, const char* path) {
+  EH_CHECK_ARG(gh && path, "graph/path is NULL");
+  HostGraph* g = HG(gh);
+  FILE* f = fopen(path, "wb");
+  if (!f) return set_error(EH_ERR_IO, "cannot open %s for writing", path);
+  bool ok = fwrite(&g->n, sizeof(uint64_t), 1, f) == 1;
+  for (uint64_t i = 0; i < g->n && ok; i++) {
+    uint64_t hdr[2] = {g->ext_ids[i], g->offsets[i + 1] - g->offsets[i]};
+    ok = fwrite(hdr, sizeof(uint64_t), 2, f) == 2;
+    if (ok && hdr[1])
+      ok = fwrite(g->nbrs.data() + g->offsets[i], sizeof(uint32_t), hdr[1], f) == hdr[1];
+  }
+  ok = (fclose(f) == 0) && ok;
+  return ok ? EH_OK : set_error(EH_ERR_IO, "write to %s failed", path);
+}
+
+eh_status eh_hgraph_read_edge_list(const char* path, eh_hgraph_t* out) {
+  EH_CHECK_ARG(path && out, "path/out is NULL");
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return set_error(EH_ERR_IO, "cannot open %s", path);
+  std::string text((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+  // Tokens are separated by ' ', '\t', '\n' or 'A', as the reference's strtok call.
+  std::vector<uint64_t> tok;
+  size_t p = 0, L = text.size();
+  auto is_sep = [](char c) { return c == ' ' || c == '\t' || c == '\n' || c == 'A'; };
+  while (p < L) {
+    while (p < L && is_sep(text[p])) p++;
+    if (p >= L) break;
+    size_t q = p;
+    while (q < L && !is_sep(text[q])) q++;
+    tok.push_back(strtoull(text.c_str() + p, nullptr, 10));
+    p = q;
+  }
+  if (tok.size() % 2) return set_error(EH_ERR_IO, "%s: odd number of ids", path);
+  std::unordered_map<uint64_t, uint32_t> ids;
+  std::vector<uint64_t> id_map;
+  std::vector<std::vector<uint32_t>> rows;
+  auto intern = [&](uint64_t x) -> uint32_t {
+    auto it = ids.find(x);
+    if (it != ids.end()) return it->second;
+    uint32_t id = (uint32_t)id_map.size();
+    ids.emplace(x, id);
+    id_map.push_back(x);
+    rows.emplace_back();
+    return id;
+  };
+  for (size_t t = 0; t < tok.size(); t += 2) {
+    uint32_t s = intern(tok[t]);
+    uint32_t d = intern(tok[t + 1]);
+    rows[s].push_back(d);
+    rows[d].push_back(s);
+  }
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  g->n = rows.size();
+  g->offsets.assign(g->n + 1, 0);
+  for (uint64_t i = 0; i < g->n; i++) {
+    auto& r = rows[i];
+    std::sort(r.begin(), r.end());
+    // The reference takes the maximum row size before removing duplicates.
+    g->max_nbrhood_size = std::max<uint64_t>(g->max_nbrhood_size, r.size());
+    r.erase(std::unique(r.begin(), r.end()), r.end());
+    g->offsets[i + 1] = g->offsets[i] + r.size();
+  }
+  g->nbrs.reserve(g->offsets[g->n]);
+  for (auto& r : rows) g->nbrs.insert(g->nbrs.end(), r.begin(), r.end());
+  g->ext_ids = id_map;
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
+}
+
+eh_status eh_hgraph_reorder_by_degree(eh_hgraph_t gh) {
+  EH_CHECK_ARG(gh, "graph is NULL");
+  HostGraph* g = HG(gh);
+  const uint64_t n = g->n;
+  std::vector<uint32_t> new2old(n);
+  std::iota(new2old.begin(), new2old.end(), 0);
+  const uint64_t* off = g->offsets.data();
+  // Descending degree, ties by ascending old id: a strict total order, so any
+  // correct sort gives the same permutation as the reference's std::sort.
+  __gnu_parallel::sort(new2old.begin(), new2old.end(), [off](uint32_t a, uint32_t b) {
+    uint64_t da = off[a + 1] - off[a], db = off[b + 1] - off[b];
+    return da != db ? da > db : a < b;
+  });
+  std::vector<uint32_t> old2new(n);
+  for (uint64_t i = 0; i < n; i++) old2new[new2old[i]] = (uint32_t)i;
+  std::vector<uint64_t> noff(n + 1, 0);
+  for (uint64_t i = 0; i < n; i++) noff[i + 1] = noff[i] + (off[new2old[i] + 1] - off[new2old[i]]);
+  std::vector<uint32_t> nnbr(g->nbrs.size());
+  std::vector<uint64_t> next(n);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t i = 0; i < (int64_t)n; i++) {
+    uint32_t o = new2old[i];
+    uint64_t dst = noff[i];
+    for (uint64_t e = off[o]; e < off[o + 1]; e++) nnbr[dst++] = old2new[g->nbrs[e]];
+    std::sort(nnbr.begin() + noff[i], nnbr.begin() + noff[i + 1]);
+    next[i] = g->ext_ids[o];
+  }
+  g->offsets.swap(noff);
+  g->nbrs.swap(nnbr);
+  g->ext_ids.swap(next);
+  return EH_OK;
+}
+
+eh_status eh_hgraph_view(eh_hgraph_t gh, uint64_t* n, uint64_t* num_edges, const uint64_t** offsets,
+                         const uint32_t** nbrs, const uint64_t** ext_ids,
+                         uint64_t* max_nbrhood_size) {
+  EH_CHECK_ARG(gh, "graph is NULL");
+  HostGraph* g = HG(gh);
+  if (n) *n = g->n;
+  if (num_edges) *num_edges = g->offsets[g->n];
+  if (offsets) *offsets = g->offsets.data();
+  if (nbrs) *nbrs = g->nbrs.data();
+  if (ext_ids) *ext_ids = g->ext_ids.data();
+  if (max_nbrhood_size) *max_nbrhood_size = g->max_nbrhood_size;
+  return EH_OK;
+}
+
+void eh_hgraph_free(eh_hgraph_t g) { delete HG(g); }
+
+eh_status eh_generate_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c,
+                           uint64_t seed, eh_hgraph_t* out) {
+  EH_CHECK_ARG(out, "out is NULL");
+  EH_CHECK_ARG(scale >= 1 && scale <= 31, "scale %u out of range [1,31]", scale);
+  EH_CHECK_ARG(a >= 0 && b >= 0 && c >= 0 && a + b + c <= 1.0, "bad R-MAT probabilities");
+  const uint64_t n = 1ULL << scale;
+  EH_CHECK_ARG(num_edges <= n * (n - 1) / 2, "more edges than vertex pairs");
+  // Quadrant thresholds on the top 53 bits of each draw.
+  const double two53 = 9007199254740992.0;
+  const uint64_t t1 = (uint64_t)(a * two53), t2 = (uint64_t)((a + b) * two53),
+                 t3 = (uint64_t)((a + b + c) * two53);
+  eh::Stream st(seed, 0x524D4154ULL /* "RMAT" */);
+  auto draw = [&](uint64_t lo, uint64_t hi, uint64_t* dst) {
+#pragma omp parallel for schedule(static)
+    for (int64_t k = (int64_t)lo; k < (int64_t)hi; k++) {
+      uint64_t u = 0, v = 0;
+      for (uint32_t l = 0; l < scale; l++) {
+        uint64_t r = st.at((uint64_t)k * scale + l) >> 11;
+        uint64_t bu = r >= t2, bv = (r >= t1 && r < t2) || r >= t3;
+        u = (u << 1) | bu;
+        v = (v << 1) | bv;
+      }
+      dst[k - lo] = (u == v) ? eh::kSelfLoop : eh::ukey(u, v);
+    }
+  };
+  std::vector<uint64_t> keys;
+  if (!eh::first_distinct(num_edges, num_edges + num_edges / 2, draw, keys))
+    return set_error(EH_ERR_INVALID_ARGUMENT, "R-MAT could not reach %llu distinct edges",
+                     (unsigned long long)num_edges);
+  return eh::finish_graph(n, keys, out);
+}
+
+eh_status eh_generate_er(uint64_t n, uint64_t num_edges, uint64_t seed, eh_hgraph_t* out) {
+  EH_CHECK_ARG(out, "out is NULL");
+  EH_CHECK_ARG(n >= 2 && n < (1ULL << 32), "n out of range");
+  EH_CHECK_ARG(num_edges <= n * (n - 1) / 2, "more edges than vertex pairs");
+  eh::Stream st(seed, 0x4552ULL /* "ER" */);
+  auto draw = [&](uint64_t lo, uint64_t hi, uint64_t* dst) {
+#pragma omp parallel for schedule(static)
+    for (int64_t k = (int64_t)lo; k < (int64_t)hi; k++) {
+      uint64_t u = eh::bounded(st.at(2 * (uint64_t)k), n);
+      uint64_t v = eh::bounded(st.at(2 * (uint64_t)k + 1), n);
+      dst[k - lo] = (u == v) ? eh::kSelfLoop : eh::ukey(u, v);
+    }
+  };
+  std::vector<uint64_t> keys;
+  if (!eh::first_distinct(num_edges, num_edges + num_edges / 8 + 64, draw, keys))
+    return set_error(EH_ERR_INVALID_ARGUMENT, "ER could not reach %llu distinct edges",
+                     (unsigned long long)num_edges);
+  return eh::finish_graph(n, keys, out);
+}
+
+eh_status eh_generate_ba(uint64_t n, uint32_t m, uint64_t seed, eh_hgraph_t* out) {
+  EH_CHECK_ARG(out, "out is NULL");
+  EH_CHECK_ARG(m >= 1 && n > (uint64_t)m + 1 && n < (1ULL << 32), "need n > m+1 >= 2");
+  eh::Stream st(seed, 0x4241ULL /* "BA" */);
+  std::vector<uint64_t> keys;
+  std::vector<uint32_t> ends;  // every edge contributes both endpoints
+  // Seed clique on vertices 0..m.
+  for (uint32_t u = 0; u <= m; u++)
+    for (uint32_t v = u + 1; v <= m; v++) {
+      keys.push_back(eh::ukey(u, v));
+      ends.push_back(u);
+      ends.push_back(v);
+    }
+  uint64_t ctr = 0;
+  std::vector<uint32_t> picked;
+  for (uint64_t v = m + 1; v < n; v++) {
+    picked.clear();
+    while (picked.size() < m) {
+      uint32_t t = ends[eh::bounded(st.at(ctr++), ends.size())];
+      if (std::find(picked.begin(), picked.end(), t) == picked.end()) picked.push_back(t);
+    }
+    for (uint32_t t : picked) {
+      keys.push_back(eh::ukey(t, v));
+      ends.push_back(t);
+      ends.push_back((uint32_t)v);
+    }
+  }
+  std::sort(keys.begin(), keys.end());
+  return eh::finish_graph(n, keys, out);
+}
+
+eh_status eh_generate_planted_cliques(uint64_t n, uint64_t background_edges, uint32_t num_cliques,
+                                      uint32_t min_size, uint32_t max_size, uint64_t seed,
+                                      eh_hgraph_t* out) {
+  EH_CHECK_ARG(out, "out is NULL");
+  EH_CHECK_ARG(min_size >= 2 && min_size <= max_size && max_size <= n, "bad clique sizes");
+  eh_hgraph_t bg = nullptr;
+  eh_status s = eh_generate_er(n, background_edges, seed, &bg);
+  if (s != EH_OK) return s;
+  HostGraph* g = HG(bg);
+  std::vector<uint64_t> keys;
+  keys.reserve(g->nbrs.size() / 2);
+  for (uint64_t u = 0; u < n; u++)
+    for (uint64_t e = g->offsets[u]; e < g->offsets[u + 1]; e++)
+      if (g->nbrs[e] > u) keys.push_back((u << 32) | g->nbrs[e]);
+  eh_hgraph_free(bg);
+  // Discrete log-uniform sizes: P(s) proportional to 1/s on [min_size, max_size].
+  std::vector<double> cdf(max_size - min_size + 1);
+  double acc = 0.0;
+  for (uint32_t s2 = min_size; s2 <= max_size; s2++) {
+    acc += 1.0 / (double)s2;
+    cdf[s2 - min_size] = acc;
+  }
+  eh::Stream st(seed, 0x434C51ULL /* "CLQ" */);
+  uint64_t ctr = 0;
+  std::vector<uint32_t> members;
+  std::unordered_set<uint32_t> seen;
+  for (uint32_t q = 0; q < num_cliques; q++) {
+    double u = (double)(st.at(ctr++) >> 11) * (1.0 / 9007199254740992.0) * acc;
+    uint32_t size = min_size + (uint32_t)(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
+    if (size > max_size) size = max_size;
+    members.clear();
+    seen.clear();
+    while (members.size() < size) {
+      uint32_t v = (uint32_t)eh::bounded(st.at(ctr++), n);
+      if (seen.insert(v).second) members.push_back(v);
+    }
+    for (size_t x = 0; x < members.size(); x++)
+      for (size_t y = x + 1; y < members.size(); y++) keys.push_back(eh::ukey(members[x], members[y]));
+  }
+  __gnu_parallel::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  return eh::finish_graph(n, keys, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,35 @@
+// Internal helpers shared by the host (.cpp) and device (.cu) translation units.
+#pragma once
+
+#include <cstdarg>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/eh_gb300.h"
+
+namespace eh {
+
+// Records a message for eh_last_error() and returns the status unchanged.
+eh_status set_error(eh_status s, const char* fmt, ...);
+void clear_error();
+
+// Host graph behind eh_hgraph_t: CSR adjacency of a symmetric graph.
+struct HostGraph {
+  uint64_t n = 0;
+  std::vector<uint64_t> offsets;  // n+1
+  std::vector<uint32_t> nbrs;     // offsets[n]
+  std::vector<uint64_t> ext_ids;  // n
+  uint64_t max_nbrhood_size = 0;  // as the reference reports it (pre-dedup for edge lists)
+};
+
+// Builds a symmetric CSR from distinct undirected keys (lo << 32 | hi, lo < hi).
+// `keys` is consumed.  Rows come out sorted ascending.
+void csr_from_undirected_keys(uint64_t n, std::vector<uint64_t>& keys, HostGraph& g);
+
+}  // namespace eh
+
+#define EH_CHECK_ARG(cond, ...)                                      \
+  do {                                                               \
+    if (!(cond)) return eh::set_error(EH_ERR_INVALID_ARGUMENT, __VA_ARGS__); \
+  } while (0)

@@ -1,0 +1,92 @@
+// Kernel declarations shared between the build / count translation units and
+// the C-ABI layer.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "eh_device.cuh"
+
+namespace eh {
+
+// Device error flag bits (set by kernels, read by the host after a launch).
+enum : uint32_t {
+  ERRF_UNSORTED = 1u,      // a row is not strictly ascending
+  ERRF_RANGE = 2u,         // a neighbour id >= n
+  ERRF_ROW_TOO_LONG = 4u,  // a row exceeds the 2^30 element limit of RowDesc
+  ERRF_PSHORT_PART = 8u,   // a pshort partition would exceed 65536 elements
+};
+
+// Per-row measurements produced by the build's first pass.
+struct RowMeasure {
+  uint32_t card;   // selected elements
+  uint32_t aux;    // bitset: first word; pshort: partitions
+  uint32_t lt;     // type | length (RowDesc::lt)
+  uint32_t units;  // payload size in 16-byte units
+};
+
+struct BuildTotals {  // accumulated with atomics by the measure pass
+  unsigned long long cardinality;
+  unsigned long long ref_bytes;  // reference flattened bytes of all rows
+  unsigned long long num_uint, num_pshort, num_bitset;
+  unsigned long long max_full_degree;
+  unsigned long long max_card;
+  unsigned long long payload_units;
+};
+
+// eh_build.cu
+cudaError_t launch_measure(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
+                           int sel, int layout, RowMeasure* meas, BuildTotals* totals,
+                           uint32_t* err, cudaStream_t st);
+cudaError_t launch_scan_units(uint64_t n, const RowMeasure* meas, uint32_t* off16, uint32_t* block_tmp,
+                              uint64_t n_block_tmp, cudaStream_t st);
+uint64_t scan_tmp_words(uint64_t n);
+cudaError_t launch_encode(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
+                          int sel, const RowMeasure* meas, const uint32_t* off16, RowDesc* desc,
+                          uint4* arena, cudaStream_t st);
+// Work plan: rows with card >= min_card sorted by descending card.
+// hist: 65536 + scan_tmp_words(65536) words; after the call hist[0..65536) holds
+// the bin starts and cursor[0..65536) the bin ends (bin b = card 65535 - b).
+cudaError_t launch_plan(uint64_t n, const RowDesc* desc, uint32_t min_card, uint32_t* hist,
+                        uint32_t* order, uint32_t* cursor, cudaStream_t st);
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint64_t n, uint32_t* out, uint32_t* tmp,
+                               cudaStream_t st);
+cudaError_t launch_decode_rows(const RowDesc* desc, const uint4* arena, const uint32_t* rows,
+                               const unsigned long long* dst_off, uint32_t nrows, uint32_t* dst,
+                               cudaStream_t st);
+cudaError_t launch_triangle_bytes(uint64_t n, const RowDesc* desc, const uint4* arena,
+                                  unsigned long long* out, cudaStream_t st);
+
+// eh_count.cu
+struct PivotArgs {
+  const RowDesc* desc;
+  const uint4* arena;
+  const uint32_t* order;   // rows sorted by descending card
+  uint32_t n_order;        // rows in the plan
+  uint32_t n_heavy;        // order[0, n_heavy) are processed CTA-wide
+  uint32_t n_giant;        // order[0, n_giant) have decoded lists in giant_lists
+  const uint32_t* giant_lists;
+  const unsigned long long* giant_off;
+  uint32_t* counters;      // [0] next heavy unit, [1] next light chunk
+  unsigned long long* out; // result
+};
+constexpr uint32_t kCtaThreads = 256;
+constexpr uint32_t kLightMax = 96;     // pivots with card <= kLightMax run warp-wide
+constexpr uint32_t kCtaListCap = 6144; // CTA-staged list capacity (elements)
+constexpr uint32_t kCtaWordCap = 2048; // CTA-staged bitset words capacity
+cudaError_t launch_pivot_units(const RowDesc* desc, const uint32_t* order, uint32_t n_heavy,
+                               uint32_t* cnt, cudaStream_t st);
+cudaError_t launch_pivot_unit_fill(const uint32_t* cnt, const uint32_t* start, uint32_t n_heavy,
+                                   uint2* units, cudaStream_t st);
+cudaError_t launch_triangles(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
+                             cudaStream_t st);
+cudaError_t launch_lollipops(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
+                             cudaStream_t st);
+int pivot_grid(int device);
+cudaError_t launch_similar(uint64_t n, const RowDesc* desc, const uint4* arena, uint32_t vstar,
+                           uint32_t threshold, unsigned long long* out, cudaStream_t st);
+cudaError_t launch_intersect_rows(uint64_t n, const RowDesc* desc, const uint4* arena, const uint32_t* a,
+                                  const uint32_t* b, uint64_t np, uint32_t* counts, cudaStream_t st);
+cudaError_t launch_max_row(uint64_t n, const RowDesc* desc, unsigned long long* out, cudaStream_t st);
+
+}  // namespace eh

@@ -1,0 +1,138 @@
+"""CUDA path vs the oracle, through the C ABI, on seeded graphs.
+
+Counts are integers: the bar is exact equality (tolerance 0).  Every layout the
+reference offers (uint, pshort, bs, hybrid) plus the optional three-tier
+hybrid is covered, with graphs that exercise uint, bitset and pshort rows,
+empty rows, hubs split across CTAs, and rows long enough to need the decoded
+giant-pivot path.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GRAPHS = {
+    "rmat10": ("rmat", 11, dict(scale=10, edges=6000)),
+    "rmat12": ("rmat", 12, dict(scale=12, edges=40000)),
+    "er": ("er", 13, dict(n=3000, edges=30000)),
+    "ba": ("ba", 14, dict(n=4000, m=8)),
+    "planted": ("planted", 15, dict(n=6000, edges=20000, cliques=6, min_size=20, max_size=120)),
+    "dense": ("er", 16, dict(n=400, edges=40000)),
+}
+LAYOUTS = ["hybrid", "uint", "bs", "pshort", "hybrid3"]
+
+_cache = {}
+
+
+def csr(eh, name):
+    if name not in _cache:
+        kind, seed, kw = GRAPHS[name]
+        g = eh.graph(kind, seed, **kw)
+        _cache[name] = g.csr()[:2]
+    return _cache[name]
+
+
+@pytest.mark.parametrize("name", list(GRAPHS))
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_triangles(eh, oracle, name, layout):
+    off, nbr = csr(eh, name)
+    m = eh.Matrix.build(off, nbr, selection="lower", layout=layout)
+    o = oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.LAYOUTS[layout])
+    assert m.count_triangles() == o.triangles()
+
+
+@pytest.mark.parametrize("name", list(GRAPHS))
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_lollipops_and_similar(eh, oracle, name, layout):
+    off, nbr = csr(eh, name)
+    m = eh.Matrix.build(off, nbr, selection="all", layout=layout)
+    o = oracle.Matrix(off, nbr, oracle.SELECT_ALL, oracle.LAYOUTS[layout])
+    assert m.count_lollipops() == o.lollipops()
+    assert m.max_row_id() == o.max_row_id()
+    for thr in (0, 10, 50):
+        assert m.similar_nodes(thr) == o.similar_nodes(thr)
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+@pytest.mark.parametrize("selection", ["lower", "all"])
+def test_row_bytes_match_reference_format(eh, oracle, layout, selection):
+    off, nbr = csr(eh, "planted")
+    m = eh.Matrix.build(off, nbr, selection=selection, layout=layout)
+    o = oracle.Matrix(off, nbr, oracle.SELECTIONS[selection], oracle.LAYOUTS[layout])
+    info, oinfo = m.info(), o.info()
+    for k in ("matrix_size", "cardinality", "row_total_bytes_used", "num_uint_rows",
+              "num_pshort_rows", "num_bitset_rows"):
+        assert info[k] == oinfo[k], k
+    t, c, b = m.row_meta()
+    ot, oc, ob = o.row_meta()
+    assert np.array_equal(c, oc)
+    assert np.array_equal(b, ob)
+    nonempty = c > 0
+    assert np.array_equal(t[nonempty], ot[nonempty])
+    rng = np.random.default_rng(3)
+    rows = np.concatenate([np.argsort(-c.astype(np.int64))[:20], rng.integers(0, len(c), 60)])
+    for r in rows:
+        assert m.export_row(int(r)) == o.row_bytes(int(r)), int(r)
+
+
+def test_intersect_rows_all_layout_pairs(eh, oracle):
+    torch = pytest.importorskip("torch")
+    off, nbr = csr(eh, "planted")
+    for layout in LAYOUTS:
+        m = eh.Matrix.build(off, nbr, selection="all", layout=layout)
+        o = oracle.Matrix(off, nbr, oracle.SELECT_ALL, oracle.LAYOUTS[layout])
+        rng = np.random.default_rng(5)
+        n = len(off) - 1
+        a = rng.integers(0, n, 5000).astype(np.uint32)
+        b = rng.integers(0, n, 5000).astype(np.uint32)
+        a[:100] = np.arange(100)  # hubs against everything
+        da = torch.from_numpy(a.astype(np.int32)).cuda()
+        db = torch.from_numpy(b.astype(np.int32)).cuda()
+        dc = torch.zeros(len(a), dtype=torch.int32, device="cuda")
+        m.intersect_rows(da.data_ptr(), db.data_ptr(), len(a), dc.data_ptr())
+        torch.cuda.synchronize()
+        got = dc.cpu().numpy().astype(np.uint32)
+        assert np.array_equal(got, o.intersect_rows(a, b)), layout
+
+
+def test_rejects_unsorted_rows_without_fault(eh):
+    off = np.array([0, 2, 4, 6], np.uint64)
+    nbr = np.array([2, 1, 0, 2, 0, 1], np.uint32)  # row 0 descending
+    with pytest.raises(eh.EHError) as ei:
+        eh.Matrix.build(off, nbr, selection="lower", layout="hybrid")
+    assert ei.value.status == 1
+    nbr2 = np.array([1, 7, 0, 2, 0, 1], np.uint32)  # id out of range
+    with pytest.raises(eh.EHError):
+        eh.Matrix.build(off, nbr2, selection="all", layout="uint")
+    # the context is still usable afterwards
+    m = eh.Matrix.build(off, np.array([1, 2, 0, 2, 0, 1], np.uint32), selection="lower", layout="hybrid")
+    assert m.count_triangles() == 1
+
+
+def test_empty_and_tiny_graphs(eh, oracle):
+    for off, nbr in [(np.zeros(1, np.uint64), np.zeros(0, np.uint32)),
+                     (np.zeros(5, np.uint64), np.zeros(0, np.uint32)),
+                     (np.array([0, 1, 2], np.uint64), np.array([1, 0], np.uint32))]:
+        for layout in LAYOUTS:
+            m = eh.Matrix.build(off, nbr, selection="lower", layout=layout)
+            assert m.count_triangles() == 0
+            f = eh.Matrix.build(off, nbr, selection="all", layout=layout)
+            assert f.count_lollipops() == 0
+            o = oracle.Matrix(off, nbr, oracle.SELECT_ALL, oracle.LAYOUTS[layout])
+            assert f.similar_nodes(0) == o.similar_nodes(0)
+
+
+@pytest.mark.parametrize("layout", ["uint", "hybrid"])
+def test_config1_graph_with_giant_pivots(eh, oracle, layout):
+    """The 2^16-vertex, 1M-edge R-MAT graph: hubs of >6144 entries take the
+    decoded giant-pivot path in the full-row (lollipop) matrix."""
+    g = eh.graph("rmat", 1, scale=16, edges=1000000)
+    off, nbr = g.csr()[:2]
+    low = eh.Matrix.build(off, nbr, selection="lower", layout=layout)
+    olow = oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.LAYOUTS[layout])
+    assert low.count_triangles() == olow.triangles()
+    full = eh.Matrix.build(off, nbr, selection="all", layout=layout)
+    assert full.info()["max_row_cardinality"] > 6144
+    ofull = oracle.Matrix(off, nbr, oracle.SELECT_ALL, oracle.LAYOUTS[layout])
+    assert full.count_lollipops() == ofull.lollipops()
+    assert full.similar_nodes(10) == ofull.similar_nodes(10)
