@@ -147,6 +147,10 @@ eh_status eh_matrix_row_meta(eh_matrix_t m, uint8_t* types, uint32_t* cards, uin
  * written if cap is too small (EH_ERR_INVALID_ARGUMENT). */
 eh_status eh_matrix_export_row(eh_matrix_t m, uint32_t row, uint8_t* buf, uint64_t cap,
                                uint64_t* nbytes);
+/* Every row's flattened bytes back to back in row order (the contents of the
+ * reference's row_arrays, src/SparseMatrix.hpp:406-494).  Call with buf=NULL to
+ * get the size in *nbytes; EH_ERR_INVALID_ARGUMENT if cap is too small. */
+eh_status eh_matrix_export_flattened(eh_matrix_t m, uint8_t* buf, uint64_t cap, uint64_t* nbytes);
 /* SparseMatrix::get_max_row_id (src/SparseMatrix.hpp:133-145). */
 eh_status eh_matrix_get_max_row_id(eh_matrix_t m, uint32_t* row);
 /* Algorithmic bytes of one triangle-count pass:

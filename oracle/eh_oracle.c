@@ -729,3 +729,23 @@ uint64_t oracle_triangles_range(void* mp, uint64_t lo, uint64_t hi, int nthreads
 }
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+/* All rows in the row-dump format of oracle/ref_rowdump.cpp: per row u8 type,
+ * u32 cardinality, u64 flattened bytes, then those bytes.  Returns the size;
+ * writes only when buf != NULL. */
+uint64_t oracle_dump(void* mp, uint8_t* buf) {
+  omatrix* m = (omatrix*)mp;
+  uint64_t pos = 0;
+  for (uint64_t i = 0; i < m->n; i++) {
+    oset s = get_row(m, i);
+    uint64_t nb = m->row_offsets[i + 1] - m->row_offsets[i];
+    if (buf) {
+      buf[pos] = (uint8_t)s.type;
+      wr32(buf + pos + 1, m->row_lengths[i]);
+      wr64(buf + pos + 5, nb);
+      memcpy(buf + pos + 13, m->row_data + m->row_offsets[i], nb);
+    }
+    pos += 13 + nb;
+  }
+  return pos;
+}

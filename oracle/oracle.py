@@ -62,6 +62,8 @@ def lib():
         L.oracle_triangles_range.restype = C.c_uint64
         L.oracle_triangles_range.argtypes = [P, C.c_uint64, C.c_uint64, C.c_int]
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_dump.restype = C.c_uint64
+        L.oracle_dump.argtypes = [P, P]
         _lib = L
     return _lib
 
@@ -108,6 +110,13 @@ class Matrix:
 
     def max_row_id(self):
         return int(lib().oracle_max_row_id(self.h))
+
+    def dump(self):
+        """All rows in the format of oracle/ref_rowdump.cpp (type, card, bytes, payload)."""
+        size = lib().oracle_dump(self.h, None)
+        buf = np.zeros(max(1, size), np.uint8)
+        lib().oracle_dump(self.h, _ptr(buf))
+        return bytes(buf[:size])
 
     def triangles(self):
         return int(lib().oracle_triangles(self.h, self.threads))

@@ -80,6 +80,7 @@ def load(build_if_missing=True):
         "eh_matrix_get_info": (I, [P, C.POINTER(MatrixInfo)]),
         "eh_matrix_row_meta": (I, [P, P, P, P]),
         "eh_matrix_export_row": (I, [P, U32, P, U64, C.POINTER(U64)]),
+        "eh_matrix_export_flattened": (I, [P, P, U64, C.POINTER(U64)]),
         "eh_matrix_get_max_row_id": (I, [P, C.POINTER(U32)]),
         "eh_matrix_triangle_bytes": (I, [P, C.POINTER(U64)]),
         "eh_matrix_free": (None, [P]),
@@ -250,6 +251,27 @@ class Matrix:
         check(load().eh_matrix_export_row(self.h, row, _p(buf), len(buf), C.byref(nb)))
         del st
         return bytes(buf[:nb.value])
+
+    def export_flattened(self):
+        """All rows' flattened bytes back to back (the reference's row_arrays contents)."""
+        nb = C.c_uint64()
+        check(load().eh_matrix_export_flattened(self.h, None, 0, C.byref(nb)))
+        buf = np.zeros(max(1, nb.value), np.uint8)
+        check(load().eh_matrix_export_flattened(self.h, _p(buf), len(buf), C.byref(nb)))
+        return bytes(buf[:nb.value])
+
+    def dump(self):
+        """All rows in the format of oracle/ref_rowdump.cpp (type, card, bytes, payload)."""
+        t, c, b = self.row_meta()
+        flat = self.export_flattened()
+        out = bytearray()
+        pos = 0
+        for i in range(len(t)):
+            nb = int(b[i])
+            out += bytes([int(t[i])]) + int(c[i]).to_bytes(4, "little") + nb.to_bytes(8, "little")
+            out += flat[pos:pos + nb]
+            pos += nb
+        return bytes(out)
 
     def max_row_id(self):
         r = C.c_uint32()

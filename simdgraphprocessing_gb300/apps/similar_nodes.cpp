@@ -1,0 +1,47 @@
+// similar_nodes<T,R> (the reference's apps/similar_nodes.cpp): same class,
+// members and output line; rows sharing more than N neighbours with the
+// largest row, counted on the device.
+#include "emptyheaded.hpp"
+
+template <class T, class R>
+class similar_nodes : public application<T, R> {
+ public:
+  size_t count;
+  size_t N;
+
+  similar_nodes(Parser input_data) : application<T, R>(input_data) {
+    count = 0;
+    N = 10;
+  }
+
+  SparseMatrix<T, R>* materialize_graph() {
+    auto node_selection = [](uint32_t node, uint32_t attribute) -> bool {
+      (void)node;
+      (void)attribute;
+      return true;
+    };
+    auto edge_selection = [](uint32_t node, uint32_t nbr, uint32_t attribute) -> bool {
+      (void)attribute;
+      (void)node;
+      (void)nbr;
+      return true;
+    };
+    return SparseMatrix<T, R>::build(this->input_graph, node_selection, edge_selection, this->num_threads);
+  }
+
+  void run() {
+    this->graph = materialize_graph();
+    const double start_time = common::startClock();
+    this->graph->get_max_row_id();
+    count = this->graph->count_similar_nodes((uint32_t)N);
+    common::stopClock("similar_nodes", start_time);
+    cout << "Count: " << count << endl << endl;
+  }
+};
+
+#ifndef GOOGLE_TEST  // the entry point needs one init_app; test drivers may include several apps
+template <class T, class R>
+application<T, R>* init_app(Parser input_data) {
+  return new similar_nodes<T, R>(input_data);
+}
+#endif

@@ -1,6 +1,7 @@
 // C ABI over the device matrix: build orchestration, lazily built work plans,
 // pattern counts, and host views of rows in the reference's flattened format.
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -19,6 +20,16 @@ struct Plan {
   uint32_t n_units = 0;
   uint32_t* giant_lists = nullptr;
   unsigned long long* giant_off = nullptr;
+  std::vector<uint32_t> starts;  // bin starts: rows with card > x are order[0, starts[65535 - x])
+  // rows in the plan with card > x (x < 65535)
+  uint32_t above(uint32_t x) const { return starts.empty() ? 0 : starts[65535 - x]; }
+  // largest card <= x present in the plan (0 if none)
+  uint32_t largest_at_most(uint32_t x) const {
+    if (starts.empty()) return 0;
+    for (uint32_t b = 65535 - x; b < 65535; b++)
+      if (starts[b + 1] > starts[b]) return 65535 - b;
+    return 0;
+  }
 };
 
 struct Matrix {
@@ -35,6 +46,8 @@ struct Matrix {
   int grid = 0;
   int64_t vstar = -1;
   uint64_t device_bytes = 0;
+  uint32_t* clique_scratch = nullptr;  // global slots for the largest clique pivots
+  uint64_t clique_scratch_words = 0;
 };
 
 static eh_status cuda_fail(cudaError_t e, const char* what) {
@@ -162,6 +175,7 @@ static eh_status ensure_plan(Matrix* m, cudaStream_t st) {
   CU(cudaMemcpyAsync(&total, cursor + 65535, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "plan copy");
   CU(cudaStreamSynchronize(st), "plan");
   p.n_order = m->n ? total : 0;
+  p.starts = starts;
   p.n_heavy = m->n ? starts[65535 - kLightMax] : 0;
   p.n_giant = m->n ? starts[65535 - kCtaListCap] : 0;
   // Heavy units.
@@ -343,6 +357,36 @@ eh_status eh_matrix_row_meta(eh_matrix_t mh, uint8_t* types, uint32_t* cards, ui
   return EH_OK;
 }
 
+namespace eh {
+// Writes row d's flattened bytes (payload = its arena bytes) to p; returns the size.
+static uint64_t flatten_row(int layout, const RowDesc& d, const uint8_t* payload, uint8_t* p) {
+  const uint32_t type = desc_type(d), len = desc_len(d);
+  const uint64_t pbytes = type == TY_UINT ? 4ull * d.card : type == TY_BITSET ? 8ull * len : 2ull * len;
+  uint8_t* q = p;
+  if (is_hybrid(layout)) {
+    const uint64_t tag = type;
+    memcpy(q, &tag, 8);
+    q += 8;
+  }
+  if (type == TY_UINT) {
+    memcpy(q, payload, pbytes);
+    q += pbytes;
+  } else if (d.card) {
+    const uint32_t nb = (uint32_t)(type == TY_BITSET ? 8 + pbytes : pbytes);
+    memcpy(q, &nb, 4);
+    q += 4;
+    if (type == TY_BITSET) {
+      const uint64_t first = d.aux;
+      memcpy(q, &first, 8);
+      q += 8;
+    }
+    memcpy(q, payload, pbytes);
+    q += pbytes;
+  }
+  return (uint64_t)(q - p);
+}
+}  // namespace eh
+
 eh_status eh_matrix_export_row(eh_matrix_t mh, uint32_t row, uint8_t* buf, uint64_t cap, uint64_t* nbytes) {
   CHECK_MATRIX(mh);
   Matrix* m = MX(mh);
@@ -355,28 +399,28 @@ eh_status eh_matrix_export_row(eh_matrix_t mh, uint32_t row, uint8_t* buf, uint6
   EH_CHECK_ARG(buf != nullptr && cap >= total, "buffer too small (%llu < %llu)", (unsigned long long)cap,
                (unsigned long long)total);
   const uint32_t type = eh::desc_type(d), len = eh::desc_len(d);
-  uint64_t payload = type == eh::TY_UINT ? 4ull * d.card : type == eh::TY_BITSET ? 8ull * len : 2ull * len;
-  std::vector<uint8_t> pl(payload);
+  const uint64_t payload = type == eh::TY_UINT ? 4ull * d.card : type == eh::TY_BITSET ? 8ull * len : 2ull * len;
+  std::vector<uint8_t> pl(payload ? payload : 1);
   if (payload) CU(cudaMemcpy(pl.data(), m->arena + d.off16, payload, cudaMemcpyDeviceToHost), "payload copy");
-  uint8_t* p = buf;
-  if (eh::is_hybrid(m->layout)) {
-    uint64_t tag = type;
-    memcpy(p, &tag, 8);
-    p += 8;
-  }
-  if (type == eh::TY_UINT) {
-    memcpy(p, pl.data(), payload);
-  } else if (d.card) {
-    uint32_t nb = (uint32_t)(type == eh::TY_BITSET ? 8 + payload : payload);
-    memcpy(p, &nb, 4);
-    p += 4;
-    if (type == eh::TY_BITSET) {
-      uint64_t first = d.aux;
-      memcpy(p, &first, 8);
-      p += 8;
-    }
-    memcpy(p, pl.data(), payload);
-  }
+  eh::flatten_row(m->layout, d, pl.data(), buf);
+  return EH_OK;
+}
+
+eh_status eh_matrix_export_flattened(eh_matrix_t mh, uint8_t* buf, uint64_t cap, uint64_t* nbytes) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(nbytes, "nbytes is NULL");
+  Matrix* m = MX(mh);
+  std::vector<eh::RowDesc> d(m->n);
+  if (m->n) CU(cudaMemcpy(d.data(), m->desc, m->n * sizeof(eh::RowDesc), cudaMemcpyDeviceToHost), "desc copy");
+  uint64_t total = 0;
+  for (uint64_t i = 0; i < m->n; i++) total += eh::flattened_bytes(m->layout, d[i]);
+  *nbytes = total;
+  if (!buf) return EH_OK;
+  EH_CHECK_ARG(cap >= total, "buffer too small (%llu < %llu)", (unsigned long long)cap, (unsigned long long)total);
+  std::vector<uint8_t> arena((m->arena_units + 1) * 16);
+  CU(cudaMemcpy(arena.data(), m->arena, arena.size(), cudaMemcpyDeviceToHost), "arena copy");
+  uint64_t pos = 0;
+  for (uint64_t i = 0; i < m->n; i++) pos += eh::flatten_row(m->layout, d[i], arena.data() + 16ull * d[i].off16, buf + pos);
   return EH_OK;
 }
 
@@ -416,6 +460,7 @@ void eh_matrix_free(eh_matrix_t mh) {
   cudaFree(m->plan.units);
   cudaFree(m->plan.giant_lists);
   cudaFree(m->plan.giant_off);
+  cudaFree(m->clique_scratch);
   delete m;
 }
 
@@ -491,18 +536,59 @@ eh_status eh_intersect_rows(eh_matrix_t mh, const uint32_t* d_a, const uint32_t*
 
 eh_status eh_count_cliques_async(eh_matrix_t mh, uint32_t k, uint64_t* d_count, void* stream) {
   CHECK_MATRIX(mh);
-  (void)k;
-  (void)d_count;
-  (void)stream;
-  return set_error(EH_ERR_UNSUPPORTED, "clique counting is not built yet");
+  EH_CHECK_ARG(d_count, "d_count is NULL");
+  Matrix* m = MX(mh);
+  cudaStream_t st = ST(stream);
+  if (m->selection != EH_SELECT_LOWER)
+    return set_error(EH_ERR_UNSUPPORTED, "clique counting needs a matrix built with EH_SELECT_LOWER");
+  if (k > eh::kCliqueMaxK)
+    return set_error(EH_ERR_UNSUPPORTED, "clique size %u above the supported maximum %u", k, eh::kCliqueMaxK);
+  CU(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), st), "memset");
+  // The reference's recursion only returns a count at depth n >= 3 (apps/n_clique.cpp:41-43);
+  // for n < 3 it never reaches that depth and the count stays 0.
+  if (k < 3) return EH_OK;
+  eh_status s = eh::ensure_plan(m, st);
+  if (s != EH_OK) return s;
+  const eh::Plan& p = m->plan;
+  const uint32_t nG = p.above(eh::kCliqueSmemMax);
+  const uint32_t nB = p.above(32);
+  const uint32_t nL = p.above(k - 2);
+  eh::CliqueArgs a{m->desc, m->arena, p.order, k, reinterpret_cast<unsigned long long*>(d_count)};
+  CU(cudaMemsetAsync(m->counters, 0, 8 * sizeof(uint32_t), st), "memset");
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
+  if (nG > 0) {
+    const uint32_t cmax = (uint32_t)m->tot.max_card;
+    const int grid = (int)std::min<uint64_t>(nG, 2ull * sms);
+    const uint64_t words = eh::clique_slot_words(cmax, k) * grid;
+    if (words > m->clique_scratch_words) {
+      cudaStreamSynchronize(st);
+      cudaFree(m->clique_scratch);
+      m->clique_scratch = nullptr;
+      m->clique_scratch_words = 0;
+      CU(cudaMalloc((void**)&m->clique_scratch, words * 4), "clique scratch allocation");
+      m->clique_scratch_words = words;
+    }
+    CU(eh::launch_clique_cta(a, 0, nG, m->counters + 2, cmax, m->clique_scratch, grid, st), "clique kernel (global)");
+  }
+  if (nB > nG) {
+    const uint32_t cmax = p.largest_at_most(eh::kCliqueSmemMax);
+    const int grid = (int)std::min<uint64_t>(nB - nG, 4ull * sms);
+    CU(eh::launch_clique_cta(a, nG, nB, m->counters + 3, cmax, nullptr, grid, st), "clique kernel (shared)");
+  }
+  if (nL > nB) {
+    const int grid = (int)std::min<uint64_t>((nL - nB + 63) / 64, 8ull * sms);
+    CU(eh::launch_clique_light(a, nB, nL, m->counters + 4, grid > 0 ? grid : 1, st), "clique kernel (warp)");
+  }
+  return EH_OK;
 }
 
 eh_status eh_count_cliques(eh_matrix_t mh, uint32_t k, uint64_t* count, void* stream) {
   CHECK_MATRIX(mh);
-  (void)k;
-  (void)count;
-  (void)stream;
-  return set_error(EH_ERR_UNSUPPORTED, "clique counting is not built yet");
+  EH_CHECK_ARG(count, "count is NULL");
+  eh_status s = eh_count_cliques_async(mh, k, reinterpret_cast<uint64_t*>(MX(mh)->result), stream);
+  if (s != EH_OK) return s;
+  return eh::finish_sync(MX(mh), MX(mh)->result, count, ST(stream));
 }
 
 }  // extern "C"

@@ -1,0 +1,259 @@
+// k-clique counting: the reference's n_clique<T,R>::run / apply_function
+// (apps/n_clique.cpp:30-101).
+//
+// The reference walks, for every pivot i and j in A_i = row(i) (rows pruned to
+// nbr < node), the materialized intersection C = A_i ∩ row(j), then for each
+// k in C the intersection C ∩ row(k), and so on to depth n, returning |C| at
+// the last level.  Every set on that path is a subset of A_i, so here each is a
+// bitmask over the positions of A_i: M[e] = {t < e : A_i[t] in row(A_i[e])} is
+// A_i ∩ row(A_i[e]) (row(j) only holds ids below j), and the reference's
+// C ∩ row(k) for k = A_i[t] is M[e] & M[t].  The masks are built with the same
+// layout-aware choice as the triangle kernel (probe each A_i[t] into row(j), or
+// stream row(j) and look each element up in A_i); the counting is popcounts of
+// ANDs:
+//   k = 3: sum_e popc(M[e])
+//   k = 4: sum_e sum_{t in M[e]} popc(M[e] & M[t])
+//   k > 4: depth-first over the same masks.
+// Tiers by |A_i| (rows sorted by descending size): one warp per pivot with
+// one-word masks (|A_i| <= 32); one CTA per pivot with masks in shared memory
+// (|A_i| <= kCliqueSmemMax); one CTA per pivot with masks in a global scratch
+// slot (larger pivots).
+#include <cstdint>
+
+#include "eh_kernels.cuh"
+
+namespace eh {
+
+namespace {
+
+constexpr int NW = kCtaThreads / 32;
+
+__device__ __forceinline__ uint32_t ilog2p1_c(uint32_t x) { return 32u - __clz(x | 1u); }
+
+// ---- light tier: |A_i| <= 32, one warp per pivot, one-word masks ----
+__global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint32_t pos_begin,
+                                                              uint32_t pos_end, uint32_t* counter) {
+  __shared__ uint32_t s_list[NW][32];
+  __shared__ uint32_t s_mask[NW][32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t* list = s_list[warp];
+  uint32_t* mask = s_mask[warp];
+  const int top = (int)a.k - 3;  // DFS depth at which a popcount finishes the count
+  unsigned long long acc = 0;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(counter, 8u);
+    base = __shfl_sync(FULL, base, 0) + pos_begin;
+    if (base >= pos_end) break;
+    const uint32_t end = min(pos_end, base + 8u);
+    for (uint32_t p = base; p < end; p++) {
+      const RowView A = load_view(a.desc, a.arena, a.order[p]);
+      const uint32_t c = A.card;
+      warp_decode(A, list, lane);
+      mask[lane] = 0;
+      __syncwarp();
+      // phase 1: every (e, t < e) pair, one per lane
+      const uint32_t pairs = c * (c - 1) / 2;
+      uint32_t e = 1, t = lane;
+      while (t >= e) { t -= e; e++; }
+      for (uint32_t q = lane; q < pairs; q += 32) {
+        const RowView B = load_view(a.desc, a.arena, list[e]);
+        if (row_contains(B, list[t])) atomicOr(&mask[e], 1u << t);
+        t += 32;
+        while (t >= e && e < c) { t -= e; e++; }
+      }
+      __syncwarp();
+      // phase 2: lane e counts the cliques whose two largest members are i and A_i[e]
+      if (lane < c) {
+        const uint32_t m0 = mask[lane];
+        if (top == 0) {
+          acc += __popc(m0);
+        } else if (top == 1) {
+          uint32_t m = m0;
+          while (m) {
+            const uint32_t tt = __ffs(m) - 1;
+            m &= m - 1;
+            acc += __popc(m0 & mask[tt]);
+          }
+        } else {
+          uint32_t S[kCliqueMaxK], R[kCliqueMaxK];
+          S[0] = R[0] = m0;
+          int d = 0;
+          while (d >= 0) {
+            if (d == top) {
+              acc += __popc(S[d]);
+              d--;
+              continue;
+            }
+            if (!R[d]) {
+              d--;
+              continue;
+            }
+            const uint32_t tt = __ffs(R[d]) - 1;
+            R[d] &= R[d] - 1;
+            const uint32_t nx = S[d] & mask[tt];
+            if ((uint32_t)__popc(nx) >= (uint32_t)(top - d)) {  // enough candidates left
+              S[d + 1] = R[d + 1] = nx;
+              d++;
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  acc = warp_sum_u64(acc);
+  if (lane == 0 && acc) atomicAdd(a.out, acc);
+}
+
+// ---- CTA tiers: one pivot per CTA; masks in shared memory or a global slot ----
+// Per CTA working set (words): list[cmax] | masks[cmax * W] | stacks[NW][2 * (k-2) * W]
+template <bool GLOBAL>
+__global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32_t pos_begin, uint32_t pos_end,
+                                                            uint32_t* counter, uint32_t cmax, uint32_t W,
+                                                            uint32_t* gscratch, uint64_t slot_words) {
+  extern __shared__ __align__(16) uint32_t dyn[];
+  __shared__ uint32_t s_unit;
+  __shared__ uint32_t s_scan[kCtaThreads];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t* base = GLOBAL ? gscratch + (uint64_t)blockIdx.x * slot_words : dyn;
+  uint32_t* list = base;
+  uint32_t* masks = base + cmax;
+  const uint32_t stack_words = 2u * (a.k - 2) * W;
+  uint32_t* stack = masks + (uint64_t)cmax * W + (uint64_t)warp * stack_words;
+  const int top = (int)a.k - 3;
+  unsigned long long acc = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_unit = atomicAdd(counter, 1u) + pos_begin;
+    __syncthreads();
+    const uint32_t unit = s_unit;
+    if (unit >= pos_end) break;
+    const RowView A = load_view(a.desc, a.arena, a.order[unit]);
+    const uint32_t c = A.card;
+    cta_decode<kCtaThreads>(A, list, s_scan);
+    for (uint64_t x = threadIdx.x; x < (uint64_t)c * W; x += kCtaThreads) masks[x] = 0;
+    __syncthreads();
+    // phase 1: warp per e builds M[e]
+    for (uint32_t e = 1 + warp; e < c; e += NW) {
+      const uint32_t j = list[e];
+      const RowView B = load_view(a.desc, a.arena, j);
+      if (B.card == 0) continue;
+      uint32_t* Me = masks + (uint64_t)e * W;
+      bool stream = false;
+      if (B.type == TY_UINT) stream = (uint64_t)B.card * ilog2p1_c(e) < (uint64_t)e * ilog2p1_c(B.card) * 4u;
+      else if (B.type == TY_PSHORT) stream = (uint64_t)B.card * ilog2p1_c(e) < (uint64_t)e * (B.aux + ilog2p1_c(B.card)) * 4u;
+      if (!stream) {
+        for (uint32_t b = 0; b < e; b += 32) {
+          const uint32_t t = b + lane;
+          const bool hit = t < e && row_contains(B, list[t]);
+          const uint32_t word = __ballot_sync(FULL, hit);
+          if (lane == 0) Me[b >> 5] = word;
+        }
+      } else {
+        warp_for_each(B, j, lane, [&](uint32_t y) {
+          const uint32_t t = lower_bound_u32(list, 0, e, y);
+          if (t < e && list[t] == y) atomicOr(&Me[t >> 5], 1u << (t & 31));
+        });
+      }
+    }
+    __syncthreads();
+    // phase 2: warp per e
+    for (uint32_t e = 1 + warp; e < c; e += NW) {
+      const uint32_t* Me = masks + (uint64_t)e * W;
+      const uint32_t we = (e + 31) >> 5;  // words that can hold bits < e
+      if (top == 0) {
+        for (uint32_t w = lane; w < we; w += 32) acc += __popc(Me[w]);
+      } else if (top == 1) {
+        for (uint32_t w = 0; w < we; w++) {
+          const uint32_t bits = Me[w];
+          if (!((bits >> lane) & 1u)) continue;
+          const uint32_t t = 32 * w + lane;
+          const uint32_t* Mt = masks + (uint64_t)t * W;
+          for (uint32_t x = 0; x <= (t >> 5); x++) acc += __popc(Me[x] & Mt[x]);
+        }
+      } else {
+        // Warp-cooperative depth-first search; S[d], R[d] live in the warp's stack.
+        uint32_t* S = stack;
+        uint32_t* R = stack + (a.k - 2) * W;
+        for (uint32_t w = lane; w < W; w += 32) S[w] = R[w] = (w < we) ? Me[w] : 0u;
+        __syncwarp();
+        int d = 0;
+        while (d >= 0) {
+          uint32_t* Sd = S + (uint64_t)d * W;
+          uint32_t* Rd = R + (uint64_t)d * W;
+          if (d == top) {
+            for (uint32_t w = lane; w < W; w += 32) acc += __popc(Sd[w]);  // summed over lanes at the end
+            d--;
+            continue;
+          }
+          // lowest remaining candidate t in Rd
+          uint32_t t = 0xffffffffu;
+          for (uint32_t w0 = 0; w0 < W && t == 0xffffffffu; w0 += 32) {
+            const uint32_t w = w0 + lane;
+            const uint32_t v = w < W ? Rd[w] : 0u;
+            const uint32_t nz = __ballot_sync(FULL, v != 0);
+            if (nz) {
+              const uint32_t src = __ffs(nz) - 1;
+              const uint32_t vw = __shfl_sync(FULL, v, src);
+              t = 32 * (w0 + src) + (__ffs(vw) - 1);
+            }
+          }
+          if (t == 0xffffffffu) {
+            d--;
+            continue;
+          }
+          __syncwarp();
+          if (lane == 0) Rd[t >> 5] &= ~(1u << (t & 31));
+          const uint32_t* Mt = masks + (uint64_t)t * W;
+          uint32_t* Sn = S + (uint64_t)(d + 1) * W;
+          uint32_t* Rn = R + (uint64_t)(d + 1) * W;
+          uint32_t cnt = 0;
+          for (uint32_t w = lane; w < W; w += 32) {
+            const uint32_t v = Sd[w] & Mt[w];
+            Sn[w] = v;
+            Rn[w] = v;
+            cnt += __popc(v);
+          }
+          cnt = warp_sum_u32(cnt);
+          __syncwarp();
+          if (cnt >= (uint32_t)(top - d)) d++;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  acc = warp_sum_u64(acc);
+  if (lane == 0 && acc) atomicAdd(a.out, acc);
+}
+
+}  // namespace
+
+uint64_t clique_slot_words(uint32_t cmax, uint32_t k) {
+  const uint64_t W = (cmax + 31) / 32;
+  return (uint64_t)cmax + (uint64_t)cmax * W + (uint64_t)NW * 2 * (k - 2) * W;
+}
+
+cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
+                                int grid, cudaStream_t st) {
+  if (pos_end <= pos_begin) return cudaSuccess;
+  k_clique_light<<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
+                              uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st) {
+  if (pos_end <= pos_begin) return cudaSuccess;
+  const uint32_t W = (cmax + 31) / 32;
+  const uint64_t slot = clique_slot_words(cmax, a.k);
+  if (gscratch) {
+    k_clique_cta<true><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch, slot);
+  } else {
+    const size_t bytes = slot * 4;
+    cudaError_t e = cudaFuncSetAttribute(k_clique_cta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    k_clique_cta<false><<<grid, kCtaThreads, bytes, st>>>(a, pos_begin, pos_end, counter, cmax, W, nullptr, slot);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace eh

@@ -44,91 +44,6 @@ struct __align__(16) PivotSmem {
   uint32_t unit;
 };
 
-// CTA-cooperative decode of a row into a sorted u32 list in shared memory.
-__device__ void cta_decode(const RowView& A, uint32_t* list, uint32_t* scan) {
-  const uint32_t tid = threadIdx.x;
-  if (A.type == TY_UINT) {
-    const uint32_t* a = static_cast<const uint32_t*>(A.p);
-    for (uint32_t k = tid; k < A.card; k += kCtaThreads) list[k] = a[k];
-    return;
-  }
-  if (A.type == TY_BITSET) {
-    // Thread t owns words [t*W/T, (t+1)*W/T); exclusive scan of their popcounts
-    // gives each thread its output position.
-    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
-    const uint32_t W = A.len;
-    const uint32_t w0 = (uint32_t)(((uint64_t)W * tid) / kCtaThreads);
-    const uint32_t w1 = (uint32_t)(((uint64_t)W * (tid + 1)) / kCtaThreads);
-    uint32_t c = 0;
-    for (uint32_t k = w0; k < w1; k++) c += __popcll(w[k]);
-    scan[tid] = c;
-    __syncthreads();
-    // Hillis-Steele inclusive scan over kCtaThreads values.
-    for (uint32_t d = 1; d < kCtaThreads; d <<= 1) {
-      const uint32_t v = tid >= d ? scan[tid - d] : 0u;
-      __syncthreads();
-      scan[tid] += v;
-      __syncthreads();
-    }
-    uint32_t pos = scan[tid] - c;
-    for (uint32_t k = w0; k < w1; k++) {
-      unsigned long long x = w[k];
-      while (x) {
-        list[pos++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
-        x &= x - 1ull;
-      }
-    }
-    return;
-  }
-  if (tid < 32) {  // pshort: walk the partitions with one warp
-    const uint16_t* s = static_cast<const uint16_t*>(A.p);
-    uint32_t i = 0, pos = 0;
-    while (i < A.len) {
-      const uint32_t hb = (uint32_t)s[i] << 16, cnt = (uint32_t)s[i + 1] + 1;
-      for (uint32_t k = tid; k < cnt; k += 32) list[pos + k] = hb | s[i + 2 + k];
-      pos += cnt;
-      i += cnt + 2;
-    }
-  }
-}
-
-// Warp-cooperative decode into the warp's slice (card <= kLightMax).
-__device__ __forceinline__ void warp_decode(const RowView& A, uint32_t* list, uint32_t lane) {
-  if (A.type == TY_UINT) {
-    const uint32_t* a = static_cast<const uint32_t*>(A.p);
-    for (uint32_t k = lane; k < A.card; k += 32) list[k] = a[k];
-  } else if (A.type == TY_BITSET) {
-    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
-    uint32_t pos = 0;
-    for (uint32_t base = 0; base < A.len; base += 32) {
-      const uint32_t k = base + lane;
-      unsigned long long x = k < A.len ? w[k] : 0ull;
-      const uint32_t c = __popcll(x);
-      uint32_t inc = c;
-      for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t t = __shfl_up_sync(FULL, inc, d);
-        if (lane >= (uint32_t)d) inc += t;
-      }
-      uint32_t p = pos + inc - c;
-      while (x) {
-        list[p++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
-        x &= x - 1ull;
-      }
-      pos += __shfl_sync(FULL, inc, 31);
-    }
-  } else {
-    const uint16_t* s = static_cast<const uint16_t*>(A.p);
-    uint32_t i = 0, pos = 0;
-    while (i < A.len) {
-      const uint32_t hb = (uint32_t)s[i] << 16, cnt = (uint32_t)s[i + 1] + 1;
-      for (uint32_t k = lane; k < cnt; k += 32) list[pos + k] = hb | s[i + 2 + k];
-      pos += cnt;
-      i += cnt + 2;
-    }
-  }
-  __syncwarp();
-}
-
 __device__ __forceinline__ uint32_t ilog2p1(uint32_t x) { return 32u - __clz(x | 1u); }
 
 // |{t < e : L[t] in B}| with j = L[e]; warp-uniform result.  A is the pivot row
@@ -194,7 +109,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
     if (uu.x < a.n_giant) {
       L = (A.type == TY_UINT) ? static_cast<const uint32_t*>(A.p) : a.giant_lists + a.giant_off[uu.x];
     } else {
-      cta_decode(A, s.list, s.scan);
+      cta_decode<kCtaThreads>(A, s.list, s.scan);
       L = s.list;
     }
     if (A.type == TY_BITSET && A.len <= kCtaWordCap) {

@@ -146,12 +146,130 @@ __device__ __forceinline__ void warp_for_each(const RowView& V, uint32_t lim, ui
   }
 }
 
+// The reference's pshort ∩ pshort kernel keeps each partition's intersection
+// size in a uint16_t (intersection.hpp:857-865), so a partition pair whose
+// 65,536 values are all common adds 0 and none of those values reach its
+// output.  That needs a full 2^16 block in both rows, hence >= 65,536 entries
+// in each; pshort_pair_drop() returns how many of the dropped values lie
+// below `lim` (0 in every other case).  Run by one lane.
+__device__ inline bool pshort_full_block(const RowView& V, uint32_t h) {
+  const uint16_t* s = static_cast<const uint16_t*>(V.p);
+  uint32_t i = 0;
+  while (i < V.len) {
+    const uint32_t hh = s[i], cnt = (uint32_t)s[i + 1] + 1;
+    if (hh == h) return cnt == 65536u;
+    if (hh > h) return false;
+    i += cnt + 2;
+  }
+  return false;
+}
+__device__ inline uint64_t pshort_pair_drop(const RowView& A, const RowView& B, uint64_t lim) {
+  if (A.type != TY_PSHORT || B.type != TY_PSHORT || A.card < 65536u || B.card < 65536u) return 0;
+  const uint16_t* s = static_cast<const uint16_t*>(B.p);
+  uint64_t drop = 0;
+  uint32_t i = 0;
+  while (i < B.len) {
+    const uint32_t h = s[i], cnt = (uint32_t)s[i + 1] + 1;
+    const uint64_t lo = (uint64_t)h << 16;
+    if (lo >= lim) break;
+    if (cnt == 65536u && pshort_full_block(A, h)) drop += min((uint64_t)65536, lim - lo);
+    i += cnt + 2;
+  }
+  return drop;
+}
+
 // Layout payload bytes of a row as the algorithmic-bytes formula counts them:
 // uint 4|S|, bitset 8 (words + 1), pshort 2 (|S| + 2 partitions).
 __device__ __forceinline__ uint64_t payload_bytes(const RowView& V) {
   if (V.type == TY_UINT) return 4ull * V.card;
   if (V.type == TY_BITSET) return V.card ? 8ull * (V.len + 1) : 0ull;
   return 2ull * V.len;
+}
+
+// CTA-cooperative decode of a row into a sorted u32 list in shared memory.
+template <uint32_t kThreads>
+__device__ inline void cta_decode(const RowView& A, uint32_t* list, uint32_t* scan) {
+  const uint32_t tid = threadIdx.x;
+  if (A.type == TY_UINT) {
+    const uint32_t* a = static_cast<const uint32_t*>(A.p);
+    for (uint32_t k = tid; k < A.card; k += kThreads) list[k] = a[k];
+    return;
+  }
+  if (A.type == TY_BITSET) {
+    // Thread t owns words [t*W/T, (t+1)*W/T); exclusive scan of their popcounts
+    // gives each thread its output position.
+    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
+    const uint32_t W = A.len;
+    const uint32_t w0 = (uint32_t)(((uint64_t)W * tid) / kThreads);
+    const uint32_t w1 = (uint32_t)(((uint64_t)W * (tid + 1)) / kThreads);
+    uint32_t c = 0;
+    for (uint32_t k = w0; k < w1; k++) c += __popcll(w[k]);
+    scan[tid] = c;
+    __syncthreads();
+    // Hillis-Steele inclusive scan over kThreads values.
+    for (uint32_t d = 1; d < kThreads; d <<= 1) {
+      const uint32_t v = tid >= d ? scan[tid - d] : 0u;
+      __syncthreads();
+      scan[tid] += v;
+      __syncthreads();
+    }
+    uint32_t pos = scan[tid] - c;
+    for (uint32_t k = w0; k < w1; k++) {
+      unsigned long long x = w[k];
+      while (x) {
+        list[pos++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
+        x &= x - 1ull;
+      }
+    }
+    return;
+  }
+  if (tid < 32) {  // pshort: walk the partitions with one warp
+    const uint16_t* s = static_cast<const uint16_t*>(A.p);
+    uint32_t i = 0, pos = 0;
+    while (i < A.len) {
+      const uint32_t hb = (uint32_t)s[i] << 16, cnt = (uint32_t)s[i + 1] + 1;
+      for (uint32_t k = tid; k < cnt; k += 32) list[pos + k] = hb | s[i + 2 + k];
+      pos += cnt;
+      i += cnt + 2;
+    }
+  }
+}
+
+// Warp-cooperative decode into the warp's slice (card <= kLightMax).
+__device__ __forceinline__ void warp_decode(const RowView& A, uint32_t* list, uint32_t lane) {
+  if (A.type == TY_UINT) {
+    const uint32_t* a = static_cast<const uint32_t*>(A.p);
+    for (uint32_t k = lane; k < A.card; k += 32) list[k] = a[k];
+  } else if (A.type == TY_BITSET) {
+    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
+    uint32_t pos = 0;
+    for (uint32_t base = 0; base < A.len; base += 32) {
+      const uint32_t k = base + lane;
+      unsigned long long x = k < A.len ? w[k] : 0ull;
+      const uint32_t c = __popcll(x);
+      uint32_t inc = c;
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, inc, d);
+        if (lane >= (uint32_t)d) inc += t;
+      }
+      uint32_t p = pos + inc - c;
+      while (x) {
+        list[p++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
+        x &= x - 1ull;
+      }
+      pos += __shfl_sync(FULL, inc, 31);
+    }
+  } else {
+    const uint16_t* s = static_cast<const uint16_t*>(A.p);
+    uint32_t i = 0, pos = 0;
+    while (i < A.len) {
+      const uint32_t hb = (uint32_t)s[i] << 16, cnt = (uint32_t)s[i + 1] + 1;
+      for (uint32_t k = lane; k < cnt; k += 32) list[pos + k] = hb | s[i + 2 + k];
+      pos += cnt;
+      i += cnt + 2;
+    }
+  }
+  __syncwarp();
 }
 
 }  // namespace eh

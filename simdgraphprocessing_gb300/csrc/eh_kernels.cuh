@@ -89,4 +89,23 @@ cudaError_t launch_intersect_rows(uint64_t n, const RowDesc* desc, const uint4* 
                                   const uint32_t* b, uint64_t np, uint32_t* counts, cudaStream_t st);
 cudaError_t launch_max_row(uint64_t n, const RowDesc* desc, unsigned long long* out, cudaStream_t st);
 
+// eh_clique.cu
+struct CliqueArgs {
+  const RowDesc* desc;
+  const uint4* arena;
+  const uint32_t* order;   // rows sorted by descending card
+  uint32_t k;              // clique size, 3 <= k <= kCliqueMaxK
+  unsigned long long* out;
+};
+constexpr uint32_t kCliqueMaxK = 16;
+constexpr uint32_t kCliqueSmemMax = 1024;  // pivots up to this size keep their masks in shared memory
+// Words of one pivot's working set (list, masks, per-warp DFS stacks).
+uint64_t clique_slot_words(uint32_t cmax, uint32_t k);
+cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
+                                int grid, cudaStream_t st);
+// gscratch == nullptr: masks in dynamic shared memory; else grid slots of
+// clique_slot_words(cmax, k) words each in global memory.
+cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
+                              uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st);
+
 }  // namespace eh

@@ -1,0 +1,114 @@
+"""Regenerates tests/golden/reference_counts.json.
+
+Runs the reference's own binaries -- compiled from its unmodified sources by
+oracle/build_ref.sh into oracle/_ref/ -- on seeded generator graphs written in
+the reference's binary format, and records:
+  * the app counts per layout (undirected_triangle_counting, n_clique n=4,
+    undirected_lollipop_counting, similar_nodes), parsed from their output;
+  * a SHA-256 of the reference's encoded rows (oracle/ref_rowdump.cpp) per
+    layout and edge selection, for byte-format parity;
+  * a SHA-256 of the generated CSR, so that a host that regenerates the graph
+    (x86-64 or aarch64) can prove it got the same input.
+Needs an x86-64 host with the reference tree (the reference uses SSE/AVX).
+Usage: python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import simdgraphprocessing_gb300 as eh  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+OUT = os.path.join(HERE, "reference_counts.json")
+
+GRAPHS = [
+    {"name": "rmat_s10", "kind": "rmat", "seed": 101, "params": {"scale": 10, "edges": 8000}},
+    {"name": "rmat_s12", "kind": "rmat", "seed": 102, "params": {"scale": 12, "edges": 50000}},
+    {"name": "rmat_s14", "kind": "rmat", "seed": 103, "params": {"scale": 14, "edges": 200000}},
+    {"name": "er_2000", "kind": "er", "seed": 104, "params": {"n": 2000, "edges": 20000}},
+    {"name": "ba_3000", "kind": "ba", "seed": 105, "params": {"n": 3000, "m": 6}},
+    {"name": "planted_5000", "kind": "planted", "seed": 106,
+     "params": {"n": 5000, "edges": 15000, "cliques": 5, "min_size": 16, "max_size": 80}},
+    {"name": "dense_er_300", "kind": "er", "seed": 107, "params": {"n": 300, "edges": 20000}},
+    # The 2^16-vertex, 1M-edge R-MAT graph of the uint triangle-count workload.
+    {"name": "rmat_s16_1m", "kind": "rmat", "seed": 1, "params": {"scale": 16, "edges": 1000000}},
+]
+LAYOUTS = ["hybrid", "uint", "bs", "pshort"]
+APPS = {
+    "triangles": ("undirected_triangle_counting", r"Number of triangles:\s*(\d+)"),
+    "cliques4": ("n_clique", r"Number of cliques:\s*(\d+)"),
+    "lollipops": ("undirected_lollipop_counting", r"Count:\s*(\d+)"),
+    "similar_nodes": ("similar_nodes", r"Count:\s*(\d+)"),
+}
+
+
+def csr_sha(off, nbr):
+    h = hashlib.sha256()
+    h.update(off.astype("<u8").tobytes())
+    h.update(nbr.astype("<u4").tobytes())
+    return h.hexdigest()
+
+
+def run_app(binary, graph, layout):
+    out = subprocess.run([os.path.join(REF, binary), "--graph=" + graph, "--input_type=binary",
+                          "--t=4", "--layout=" + layout], stdout=subprocess.PIPE,
+                         stderr=subprocess.STDOUT, text=True, check=True).stdout
+    return out
+
+
+def main():
+    if not os.path.exists(os.path.join(REF, "ref_rowdump")):
+        sys.exit("oracle/_ref is not built; run: sh oracle/build_ref.sh /root/reference")
+    eh.load()
+    entries = []
+    with tempfile.TemporaryDirectory() as td:
+        for spec in GRAPHS:
+            g = eh.graph(spec["kind"], spec["seed"], **spec["params"])
+            off, nbr, _, _ = g.csr()
+            path = os.path.join(td, spec["name"] + ".bin")
+            g.write_binary(path)
+            e = dict(spec)
+            e["n"] = int(len(off) - 1)
+            e["directed_edges"] = int(len(nbr))
+            e["csr_sha256"] = csr_sha(off, nbr)
+            e["counts"] = {}
+            for layout in LAYOUTS:
+                c = {}
+                for key, (binary, pat) in APPS.items():
+                    m = re.search(pat, run_app(binary, path, layout))
+                    c[key] = int(m.group(1))
+                e["counts"][layout] = c
+            e["rows_sha256"] = {}
+            for layout in LAYOUTS:
+                for sel in ("lower", "all"):
+                    dump = os.path.join(td, "rows.bin")
+                    subprocess.run([os.path.join(REF, "ref_rowdump"), path, layout, sel, dump],
+                                   check=True, stdout=subprocess.DEVNULL)
+                    with open(dump, "rb") as f:
+                        e["rows_sha256"]["%s/%s" % (layout, sel)] = hashlib.sha256(f.read()).hexdigest()
+            print(spec["name"], e["counts"]["hybrid"], flush=True)
+            entries.append(e)
+    doc = {
+        "generated_by": "tests/golden/make_golden.py",
+        "reference_binaries": "oracle/build_ref.sh (unmodified reference sources)",
+        "reference_gtest_goldens": {
+            "source": "reference test/*.cpp on test/data/facebook.bin (hybrid layout, 4 threads)",
+            "triangles": 1612010, "cliques4": 30004668, "lollipops": 713455740, "similar_nodes": 904,
+        },
+        "graphs": entries,
+    }
+    with open(OUT, "w") as f:
+        json.dump(doc, f, indent=1, sort_keys=True)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()

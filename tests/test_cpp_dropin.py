@@ -1,0 +1,64 @@
+"""The drop-in C++ host API (simdgraphprocessing_gb300/host + apps).
+
+CPU: the reference's own gtest sources for the hot path compile unmodified
+against the drop-in headers (when the reference tree is present).
+GPU: a C++ driver that uses the app classes exactly as those gtests do runs on
+fixture graphs and must reproduce the reference binaries' counts.
+"""
+import os
+import subprocess
+import sys
+
+import pytest
+
+import _golden
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HOST = os.path.join(ROOT, "simdgraphprocessing_gb300", "host")
+APPS = os.path.join(ROOT, "simdgraphprocessing_gb300", "apps")
+CUDA_INC = "/usr/local/cuda/include"
+REF_TESTS = ["undirected_triangle_counting_test", "n_clique_test", "undirected_lollipop_counting_test",
+             "similar_nodes_test"]
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(_golden.REFERENCE_TREE, "test")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("name", REF_TESTS)
+def test_reference_gtests_compile_against_dropin_headers(name):
+    ref = _golden.REFERENCE_TREE
+    cmd = ["g++", "-std=c++11", "-fsyntax-only", "-fopenmp", "-DGOOGLE_TEST", "-I", HOST, "-I", APPS,
+           "-I", os.path.join(ref, "lib", "gtest-1.7.0", "include"), "-I", CUDA_INC,
+           os.path.join(ref, "test", name + ".cpp")]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout[-3000:]
+
+
+def _build_driver(tmp_path, eh):
+    exe = str(tmp_path / "dropin_apps")
+    libdir = os.path.dirname(eh.lib_path())
+    cmd = ["g++", "-std=c++11", "-O2", "-fopenmp", "-I", HOST, "-I", APPS, "-I", CUDA_INC,
+           os.path.join(ROOT, "tests", "cpp", "dropin_apps.cpp"), "-o", exe,
+           "-L", libdir, "-leh_gb300", "-Wl,-rpath," + libdir, "-L/usr/local/cuda/lib64", "-lcudart"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout[-3000:]
+    return exe
+
+
+def test_dropin_driver_compiles(tmp_path, eh):
+    _build_driver(tmp_path, eh)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layout", ["hybrid", "uint", "bs", "pshort"])
+def test_dropin_apps_reproduce_reference_counts(tmp_path, eh, layout):
+    exe = _build_driver(tmp_path, eh)
+    for spec in _golden.graphs()[:6]:
+        off, nbr = _golden.generate(eh, spec)
+        path = str(tmp_path / (spec["name"] + ".bin"))
+        eh.HostGraph.from_csr(off, nbr).write_binary(path)
+        want = spec["counts"][layout]
+        args = [exe, path, layout] + [str(want[k]) for k in ("triangles", "cliques4", "lollipops",
+                                                             "similar_nodes")]
+        r = subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        assert r.returncode == 0, (spec["name"], r.stdout[-2000:])
+        assert "Number of triangles: %d" % want["triangles"] in r.stdout

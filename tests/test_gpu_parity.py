@@ -136,3 +136,59 @@ def test_config1_graph_with_giant_pivots(eh, oracle, layout):
     ofull = oracle.Matrix(off, nbr, oracle.SELECT_ALL, oracle.LAYOUTS[layout])
     assert full.count_lollipops() == ofull.lollipops()
     assert full.similar_nodes(10) == ofull.similar_nodes(10)
+
+
+@pytest.mark.parametrize("name", ["rmat10", "rmat12", "er", "ba", "planted", "dense"])
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_cliques(eh, oracle, name, layout):
+    off, nbr = csr(eh, name)
+    m = eh.Matrix.build(off, nbr, selection="lower", layout=layout)
+    o = oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.LAYOUTS[layout])
+    ks = (3, 4) if name == "dense" else (3, 4, 5)
+    for k in ks:
+        assert m.count_cliques(k) == o.cliques(k), k
+
+
+def complete_graphs(sizes):
+    """Disjoint union of complete graphs K_s (vertex ids interleaved so that each
+    clique spans the id range), degree-ordered."""
+    import numpy as np
+    rng = np.random.default_rng(9)
+    n = sum(sizes)
+    perm = rng.permutation(n)
+    rows = [[] for _ in range(n)]
+    start = 0
+    for s in sizes:
+        ids = perm[start:start + s]
+        start += s
+        for v in ids:
+            rows[v] = [int(u) for u in ids if u != v]
+    off = np.zeros(n + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in rows])
+    nbr = np.array([x for r in rows for x in sorted(r)], np.uint32)
+    return off, nbr
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_cliques_closed_form_all_tiers(eh, layout):
+    from math import comb
+    sizes = [1100, 600, 200, 30, 5]  # global-scratch, shared-memory and warp tiers
+    off, nbr = complete_graphs(sizes)
+    g = eh.HostGraph.from_csr(off, nbr).reorder_by_degree()
+    off, nbr = g.csr()[:2]
+    m = eh.Matrix.build(off, nbr, selection="lower", layout=layout)
+    assert m.info()["max_row_cardinality"] > 1024
+    for k in (3, 4, 5, 6):
+        assert m.count_cliques(k) == sum(comb(s, k) for s in sizes), k
+    assert m.count_triangles() == sum(comb(s, 3) for s in sizes)
+
+
+def test_clique_size_limits(eh):
+    off, nbr = csr(eh, "rmat10")
+    m = eh.Matrix.build(off, nbr, selection="lower", layout="hybrid")
+    assert m.count_cliques(2) == 0 and m.count_cliques(1) == 0  # the reference never reaches depth n < 3
+    with pytest.raises(eh.EHError):
+        m.count_cliques(17)
+    full = eh.Matrix.build(off, nbr, selection="all", layout="hybrid")
+    with pytest.raises(eh.EHError):
+        full.count_cliques(4)

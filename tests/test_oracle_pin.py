@@ -1,0 +1,52 @@
+"""Pins the C oracle to the reference.
+
+1. The reference's own gtest goldens on test/data/facebook.bin
+   (test/undirected_triangle_counting_test.cpp:6-13, test/n_clique_test.cpp:6-12,
+   test/undirected_lollipop_counting_test.cpp:6-13, test/similar_nodes_test.cpp:6-13),
+   when the reference tree is present (it is read, never copied).
+2. Counts and encoded rows produced by the reference binaries themselves on the
+   seeded generator graphs (tests/golden/reference_counts.json, made by
+   tests/golden/make_golden.py from oracle/build_ref.sh builds).
+"""
+import hashlib
+import os
+
+import pytest
+
+import _golden
+
+FB = os.path.join(_golden.REFERENCE_TREE, "test", "data", "facebook.bin")
+LAYOUTS = ["hybrid", "uint", "bs", "pshort"]
+
+
+@pytest.mark.skipif(not os.path.exists(FB), reason="reference tree not present")
+@pytest.mark.parametrize("layout", LAYOUTS + ["hybrid3"])
+def test_facebook_gtest_goldens(oracle, layout):
+    off, nbr, _ = oracle.read_binary(FB)
+    want = _golden.load()["reference_gtest_goldens"]
+    got = oracle.counts(off, nbr, layout)
+    for k in ("triangles", "cliques4", "lollipops", "similar_nodes"):
+        assert got[k] == want[k], k
+
+
+@pytest.mark.parametrize("spec", _golden.graphs(), ids=lambda s: s["name"])
+def test_reference_fixture_counts(eh, oracle, spec):
+    off, nbr = _golden.generate(eh, spec)
+    for layout in LAYOUTS:
+        assert oracle.counts(off, nbr, layout) == spec["counts"][layout], layout
+
+
+@pytest.mark.parametrize("spec", _golden.graphs(), ids=lambda s: s["name"])
+def test_reference_fixture_row_bytes(eh, oracle, spec):
+    off, nbr = _golden.generate(eh, spec)
+    for layout in LAYOUTS:
+        for sel in ("lower", "all"):
+            m = oracle.Matrix(off, nbr, oracle.SELECTIONS[sel], oracle.LAYOUTS[layout])
+            got = hashlib.sha256(m.dump()).hexdigest()
+            assert got == spec["rows_sha256"]["%s/%s" % (layout, sel)], (layout, sel)
+
+
+def test_three_tier_mode_agrees(eh, oracle):
+    spec = _golden.graphs()[5]
+    off, nbr = _golden.generate(eh, spec)
+    assert oracle.counts(off, nbr, "hybrid3") == spec["counts"]["hybrid"]
