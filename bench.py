@@ -49,6 +49,14 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile", action="store_true", help="minimal run for ncu captures")
+    p.add_argument("--workload", default="triangles", choices=["triangles", "cliques", "batch", "serve"],
+                   help="triangles: the headline; cliques: 4-clique + lollipop on R-MAT s20 and the "
+                        "planted-clique graph; batch: 4,096 graphs in one launch vs one launch per graph; "
+                        "serve: Poisson query stream against 32 resident graphs")
+    p.add_argument("--graphs", type=int, default=0, help="batch / serve: number of graphs (0 = configured)")
+    p.add_argument("--queries", type=int, default=400, help="serve: queries in the stream")
+    p.add_argument("--rate", type=float, default=0.0, help="serve: arrivals per second (0 = 0.8 x measured capacity)")
+    p.add_argument("--slots", type=int, default=8, help="serve: concurrent queries on the device")
     return p.parse_args()
 
 
@@ -336,8 +344,189 @@ def run_ours(a, rank, world, local_rank):
         tdist.destroy_process_group()
 
 
+def _events_ms(fn, stream, reps, flush=None):
+    import torch
+    ts = []
+    for r in range(reps):
+        if flush is not None:
+            flush.fill_(r & 0xff)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return ts
+
+
+def run_cliques(a):
+    """4-clique and lollipop counts on R-MAT scale 20 ef16 seed 3 and on the
+    planted-clique graph (2^20 vertices, G(n, M) background with p = 1e-4, 1,024
+    cliques of 64..512 vertices)."""
+    import torch
+    import simdgraphprocessing_gb300 as eh
+    from simdgraphprocessing_gb300 import workloads as W
+    from oracle import oracle as O
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(1, dtype=torch.int64, device="cuda")
+    lines = []
+    for name, g in (("rmat_s20_ef16_seed3", eh.graph("rmat", 3, scale=20, edges=16 << 20)),
+                    ("planted_2^20_p1e-4_1024cliques_seed3", W.planted_graph(3))):
+        off, nbr = g.csr()[:2]
+        low = eh.Matrix.build(off, nbr, "lower", a.layout, stream=stream)
+        full = eh.Matrix.build(off, nbr, "all", a.layout, stream=stream)
+        res = {"graph": name, "pruned_edges": low.info()["cardinality"], "layout": a.layout,
+               "bitset_rows_lower": low.info()["num_bitset_rows"]}
+        c4 = low.count_cliques(4, stream=stream)
+        t4 = _events_ms(lambda: low.count_cliques_async(4, out.data_ptr(), stream.cuda_stream), stream, a.steps, flush)
+        lp = full.count_lollipops(stream=stream)
+        tl = _events_ms(lambda: full.count_lollipops_async(out.data_ptr(), stream.cuda_stream), stream, a.steps, flush)
+        res.update({"cliques4": c4, "cliques4_ms": statistics.median(t4[a.warmup:] or t4),
+                    "lollipops": lp, "lollipops_ms": statistics.median(tl[a.warmup:] or tl)})
+        if not a.no_cpu:
+            t = time.perf_counter()
+            om = O.Matrix(off, nbr, O.SELECT_LOWER, O.LAYOUTS[a.layout])
+            t = time.perf_counter()
+            oc4 = om.cliques(4)
+            res["cpu_cliques4_s"] = time.perf_counter() - t
+            res["cliques4_matches_cpu"] = oc4 == c4
+            of = O.Matrix(off, nbr, O.SELECT_ALL, O.LAYOUTS[a.layout])
+            t = time.perf_counter()
+            olp = of.lollipops()
+            res["cpu_lollipops_s"] = time.perf_counter() - t
+            res["lollipops_match_cpu"] = olp == lp
+            res["cpu_threads"] = O.lib().oracle_max_threads()
+        lines.append(res)
+    print(json.dumps({"workload": "cliques", "metric": "4-clique / lollipop count time", "unit": "ms",
+                      "higher_is_better": False, "data": "synthetic (seeded generators)", "results": lines}),
+          flush=True)
+
+
+def run_batch(a):
+    """4,096 graphs (half G(n, M), half Barabasi-Albert; n log-uniform in
+    [200, 50000]; mean degree uniform in [4, 64]; seeds 4+k): triangles and
+    4-cliques of every graph in one persistent launch each, captured in a CUDA
+    graph and replayed, with the autotuned work shape, against one launch per
+    graph on the same GPU."""
+    import torch
+    import simdgraphprocessing_gb300 as eh
+    from simdgraphprocessing_gb300 import workloads as W
+    G = a.graphs or 4096
+    t = time.perf_counter()
+    csrs, (gr, off, nbr) = W.batch_union(G, 4)
+    t_gen = time.perf_counter() - t
+    s = torch.cuda.Stream()
+    b = eh.Batch(gr, off, nbr, layout=a.layout, stream=s)
+    info = b.matrix_info()
+    tri = torch.zeros(G, dtype=torch.int64, device="cuda")
+    clq = torch.zeros(G, dtype=torch.int64, device="cuda")
+    shape = b.tune(stream=s)
+    for _ in range(a.warmup):
+        b.run(tri.data_ptr(), clq.data_ptr(), use_graph=True, stream=s)
+    s.synchronize()
+    times = _events_ms(lambda: b.run(tri.data_ptr(), clq.data_ptr(), use_graph=True, stream=s), s, a.steps)
+    batched_ms = statistics.median(times)
+    bt, bc = tri.cpu().tolist(), clq.cpu().tolist()
+    # One launch per graph (each graph its own matrix, counted on its own).
+    mats = [eh.Matrix.build(o, n, "lower", a.layout, stream=s) for o, n in csrs]
+    pt = torch.zeros(G, dtype=torch.int64, device="cuda")
+    pc = torch.zeros(G, dtype=torch.int64, device="cuda")
+    L = eh.load()
+
+    def per_graph():
+        for g, m in enumerate(mats):
+            eh.check(L.eh_count_triangles_async(m.h, C.c_void_p(pt[g:].data_ptr()), C.c_void_p(s.cuda_stream)))
+            eh.check(L.eh_count_cliques_async(m.h, 4, C.c_void_p(pc[g:].data_ptr()), C.c_void_p(s.cuda_stream)))
+
+    per_graph()
+    s.synchronize()
+    ptimes = _events_ms(per_graph, s, max(3, a.steps // 4))
+    per_ms = statistics.median(ptimes)
+    same = pt.cpu().tolist() == bt and pc.cpu().tolist() == bc
+    edges = info["cardinality"]
+    print(json.dumps({
+        "workload": "batch", "metric": "graphs counted per second (triangles + 4-cliques)", "unit": "graphs/s",
+        "value": G / (batched_ms / 1e3), "higher_is_better": True, "n_graphs": G,
+        "batched_ms": batched_ms, "per_graph_launch_ms": per_ms, "speedup_vs_per_graph": per_ms / batched_ms,
+        "counts_identical": same, "pruned_edges": edges, "edges_per_s": edges / (batched_ms / 1e3),
+        "total_triangles": int(sum(bt)), "total_cliques4": int(sum(bc)), "tuned_shape": shape,
+        "generation_s": t_gen, "data": "synthetic (seeded G(n,M) / Barabasi-Albert generators)",
+        "cuda_graph_replay": True}), flush=True)
+
+
+def run_serve(a):
+    """32 device-resident R-MAT graphs (scales 14..23, ef16, seeds 100+k); an
+    open-loop Poisson stream of triangle / 4-clique / similar_nodes queries
+    (uniform mix, uniform graph) served with continuous batching under a
+    150 GB HBM cap, against the same queries run one at a time."""
+    import random
+    import threading
+    import simdgraphprocessing_gb300 as eh
+    from simdgraphprocessing_gb300 import workloads as W
+    specs = W.serving_specs(a.graphs or 32)
+    srv = eh.Server(slots=a.slots, hbm_cap_bytes=150 << 30)
+    ids = []
+    t = time.perf_counter()
+    for scale, seed, ef in specs:
+        o, n = eh.graph("rmat", seed, scale=scale, edges=ef << scale).csr()[:2]
+        ids.append(srv.add_graph(o, n, a.layout))
+    t_load = time.perf_counter() - t
+    rnd = random.Random(5)
+    kinds = [(eh.QUERY_TRIANGLES, 0), (eh.QUERY_CLIQUES, 4), (eh.QUERY_SIMILAR_NODES, 10)]
+    mix = [(rnd.randrange(len(ids)), *kinds[rnd.randrange(3)]) for _ in range(a.queries)]
+    # One at a time: each query alone, in order (also the answers for the identity check).
+    alone = []
+    t = time.perf_counter()
+    for q in mix:
+        alone.append(srv.run_alone(ids[q[0]], q[1], q[2]))
+    serial_qps = len(mix) / (time.perf_counter() - t)
+    rate = a.rate or 0.8 * serial_qps * a.slots
+    # Open-loop Poisson arrivals from a submitter thread.
+    tickets = [None] * len(mix)
+    arrivals = []
+    tt = 0.0
+    for _ in mix:
+        tt += rnd.expovariate(rate)
+        arrivals.append(tt)
+
+    def submitter():
+        t0 = time.perf_counter()
+        for i, q in enumerate(mix):
+            d = arrivals[i] - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            tickets[i] = srv.submit(ids[q[0]], q[1], q[2])
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    res = [srv.wait(tk, timeout_ms=600000) for tk in tickets]
+    wall = time.perf_counter() - t0
+    lat = sorted((r["done_ns"] - r["submit_ns"]) / 1e6 for r in res)
+    same = all(r["count"] == c for r, c in zip(res, alone))
+    st = srv.stats()
+    srv.close()
+    qps = len(mix) / wall
+    print(json.dumps({
+        "workload": "serve", "metric": "queries/s with p50/p99 latency", "unit": "queries/s", "value": qps,
+        "higher_is_better": True, "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+        "arrival_rate_per_s": rate, "queries": len(mix), "slots": a.slots, "one_at_a_time_qps": serial_qps,
+        "speedup_vs_one_at_a_time": qps / serial_qps, "results_identical_alone_and_in_mix": same,
+        "max_inflight": st["max_inflight"], "resident_bytes": st["resident_bytes"], "hbm_cap_bytes": st["hbm_cap_bytes"],
+        "graphs": len(ids), "graph_load_s": t_load, "query_mix": "uniform: triangles / 4-cliques / similar_nodes(10)",
+        "data": "synthetic (seeded R-MAT generator)"}), flush=True)
+
+
 def main():
     a = parse_args()
+    if a.workload != "triangles":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        {"cliques": run_cliques, "batch": run_batch, "serve": run_serve}[a.workload](a)
+        return
     if a.profile:
         a.warmup, a.steps, a.no_e2e, a.no_cpu = 1, 1, True, True
     rank = int(os.environ.get("RANK", "0"))

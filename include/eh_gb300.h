@@ -184,6 +184,92 @@ eh_status eh_similar_nodes_async(eh_matrix_t m, uint32_t threshold, uint64_t* d_
 eh_status eh_intersect_rows(eh_matrix_t m, const uint32_t* d_a, const uint32_t* d_b,
                             uint64_t npairs, uint32_t* d_counts, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Work-shape autotuning (no reference counterpart).                           */
+/* ------------------------------------------------------------------------- */
+typedef struct eh_tuning {
+  uint32_t light_max;     /* pivots with at most this many entries run one per warp */
+  uint32_t unit_span;     /* pivot positions per CTA work unit for larger pivots    */
+  uint32_t ctas_per_sm;   /* resident CTAs per SM of the persistent count kernel     */
+  float ms;               /* median triangle-count time with the chosen shape        */
+  uint32_t configs_tried;
+} eh_tuning;
+/* Times the triangle count on this matrix for a small set of work shapes,
+ * coordinate by coordinate, keeps the fastest for later counts, and caches it
+ * per (GPU, layout, size bucket) in the process (and in the file named by
+ * EH_TUNE_CACHE, if set).  Matrix built with EH_SELECT_LOWER. */
+eh_status eh_matrix_tune(eh_matrix_t m, void* stream, eh_tuning* result);
+
+/* ------------------------------------------------------------------------- */
+/* Batches: many graphs counted in one launch (no reference counterpart; each   */
+/* graph's count is what the reference's apps compute for it alone).           */
+/* ------------------------------------------------------------------------- */
+typedef struct eh_batch* eh_batch_t;
+/* Graph g owns rows [graph_rows[g], graph_rows[g+1]) of one symmetric CSR over
+ * all n rows (host arrays); its neighbour ids are global row ids inside that
+ * range (an edge leaving its block is EH_ERR_INVALID_ARGUMENT). */
+eh_status eh_batch_build(uint32_t num_graphs, const uint64_t* graph_rows, uint64_t n,
+                         const uint64_t* offsets, const uint32_t* nbrs, eh_layout layout,
+                         void* stream, eh_batch_t* out);
+/* d_counts[g] (device, num_graphs entries) = k-clique count of graph g; k = 3
+ * runs the triangle kernel. */
+eh_status eh_batch_count(eh_batch_t b, uint32_t k, uint64_t* d_counts, void* stream);
+/* Triangles and 4-cliques of every graph.  use_graph != 0: the launches are
+ * captured into a CUDA graph on first use (for these output pointers) and
+ * replayed afterwards; needs a non-default stream. */
+eh_status eh_batch_run(eh_batch_t b, uint64_t* d_triangles, uint64_t* d_cliques4, int use_graph,
+                       void* stream);
+eh_status eh_batch_tune(eh_batch_t b, void* stream, eh_tuning* result);
+/* Borrowed handle of the batch's union matrix (owned by the batch). */
+eh_status eh_batch_matrix(eh_batch_t b, eh_matrix_t* m);
+void eh_batch_free(eh_batch_t b);
+
+/* ------------------------------------------------------------------------- */
+/* Serving loop (no reference counterpart).  Graphs stay resident on the       */
+/* device; queries run with continuous batching: each is launched as soon as a */
+/* slot (stream + scratch) is free and its scratch fits under the HBM cap, so  */
+/* queries arriving while others run overlap with them on the device.          */
+/* ------------------------------------------------------------------------- */
+typedef struct eh_server* eh_server_t;
+typedef struct eh_server_config {
+  uint32_t slots;          /* concurrent queries on the device (1..64)            */
+  uint64_t hbm_cap_bytes;  /* resident matrices + query scratch never exceed this */
+} eh_server_config;
+typedef enum eh_query_kind {
+  EH_QUERY_TRIANGLES = 0,     /* param unused                                    */
+  EH_QUERY_CLIQUES = 1,       /* param = clique size k                           */
+  EH_QUERY_SIMILAR_NODES = 2  /* param = threshold N (apps/similar_nodes.cpp:14) */
+} eh_query_kind;
+typedef struct eh_query_result {
+  uint64_t count;
+  int32_t status;          /* eh_status of the query                              */
+  int32_t slot;            /* slot that ran it                                    */
+  int64_t submit_ns, start_ns, done_ns;  /* steady-clock times: latency = done - submit */
+} eh_query_result;
+typedef struct eh_server_stats {
+  uint32_t graphs, slots;
+  uint64_t queued, completed, launched, max_inflight;
+  uint64_t resident_bytes, scratch_bytes, hbm_cap_bytes;
+} eh_server_counters;
+/* Starts the dispatcher thread on the current device. */
+eh_status eh_server_create(const eh_server_config* cfg, eh_server_t* out);
+/* Uploads a symmetric CSR (host arrays) and keeps both matrices the queries
+ * need resident (nbr < node rows and full rows).  EH_ERR_ADMISSION when they
+ * do not fit under the cap. */
+eh_status eh_server_add_graph(eh_server_t s, uint64_t n, const uint64_t* offsets, const uint32_t* nbrs,
+                              eh_layout layout, uint32_t* graph_id);
+eh_status eh_server_submit(eh_server_t s, uint32_t graph_id, eh_query_kind kind, uint32_t param,
+                           uint64_t* ticket);
+/* Waits at most timeout_ms (EH_ERR_TIMEOUT otherwise) and releases the ticket. */
+eh_status eh_server_wait(eh_server_t s, uint64_t ticket, uint32_t timeout_ms, eh_query_result* out);
+/* The same query run by itself on the default stream (for one-at-a-time
+ * baselines and alone-vs-mix checks); call while no submitted work is pending. */
+eh_status eh_server_run_alone(eh_server_t s, uint32_t graph_id, eh_query_kind kind, uint32_t param,
+                              uint64_t* count);
+eh_status eh_server_stats(eh_server_t s, eh_server_counters* out);
+/* Finishes queued and running queries, stops the dispatcher, frees everything. */
+void eh_server_free(eh_server_t s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,29 @@ class EHError(RuntimeError):
         self.status = status
 
 
+class Tuning(C.Structure):
+    _fields_ = [("light_max", C.c_uint32), ("unit_span", C.c_uint32), ("ctas_per_sm", C.c_uint32),
+                ("ms", C.c_float), ("configs_tried", C.c_uint32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("hbm_cap_bytes", C.c_uint64)]
+
+
+class QueryResult(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("status", C.c_int32), ("slot", C.c_int32),
+                ("submit_ns", C.c_int64), ("start_ns", C.c_int64), ("done_ns", C.c_int64)]
+
+
+class ServerCounters(C.Structure):
+    _fields_ = [("graphs", C.c_uint32), ("slots", C.c_uint32), ("queued", C.c_uint64), ("completed", C.c_uint64),
+                ("launched", C.c_uint64), ("max_inflight", C.c_uint64), ("resident_bytes", C.c_uint64),
+                ("scratch_bytes", C.c_uint64), ("hbm_cap_bytes", C.c_uint64)]
+
+
+QUERY_TRIANGLES, QUERY_CLIQUES, QUERY_SIMILAR_NODES = 0, 1, 2
+
+
 class MatrixInfo(C.Structure):
     _fields_ = [("matrix_size", C.c_uint64), ("cardinality", C.c_uint64),
                 ("row_total_bytes_used", C.c_uint64), ("max_nbrhood_size", C.c_uint64),
@@ -93,6 +116,20 @@ def load(build_if_missing=True):
         "eh_similar_nodes": (I, [P, U32, C.POINTER(U64), P]),
         "eh_similar_nodes_async": (I, [P, U32, P, P]),
         "eh_intersect_rows": (I, [P, P, P, U64, P, P]),
+        "eh_matrix_tune": (I, [P, P, C.POINTER(Tuning)]),
+        "eh_batch_build": (I, [U32, P, U64, P, P, I, P, C.POINTER(P)]),
+        "eh_batch_count": (I, [P, U32, P, P]),
+        "eh_batch_run": (I, [P, P, P, I, P]),
+        "eh_batch_tune": (I, [P, P, C.POINTER(Tuning)]),
+        "eh_batch_matrix": (I, [P, C.POINTER(P)]),
+        "eh_batch_free": (None, [P]),
+        "eh_server_create": (I, [C.POINTER(ServerConfig), C.POINTER(P)]),
+        "eh_server_add_graph": (I, [P, U64, P, P, I, C.POINTER(U32)]),
+        "eh_server_submit": (I, [P, U32, I, U32, C.POINTER(U64)]),
+        "eh_server_wait": (I, [P, U64, U32, C.POINTER(QueryResult)]),
+        "eh_server_run_alone": (I, [P, U32, I, U32, C.POINTER(U64)]),
+        "eh_server_stats": (I, [P, C.POINTER(ServerCounters)]),
+        "eh_server_free": (None, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -315,9 +352,111 @@ class Matrix:
     def similar_nodes_async(self, threshold, d_out, stream=None):
         check(load().eh_similar_nodes_async(self.h, threshold, C.c_void_p(d_out), _stream(stream)))
 
+    def tune(self, stream=None):
+        t = Tuning()
+        check(load().eh_matrix_tune(self.h, _stream(stream), C.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
     def intersect_rows(self, d_a, d_b, npairs, d_counts, stream=None):
         check(load().eh_intersect_rows(self.h, C.c_void_p(d_a), C.c_void_p(d_b), npairs,
                                        C.c_void_p(d_counts), _stream(stream)))
+
+
+class Batch:
+    """Many graphs counted in one launch (block-diagonal union of their rows)."""
+
+    def __init__(self, graph_rows, offsets, nbrs, layout="hybrid", stream=None):
+        self.graph_rows = np.ascontiguousarray(graph_rows, np.uint64)
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        nbrs = np.ascontiguousarray(nbrs, np.uint32)
+        self.num_graphs = len(self.graph_rows) - 1
+        self.h = C.c_void_p()
+        check(load().eh_batch_build(self.num_graphs, _p(self.graph_rows), len(offsets) - 1, _p(offsets),
+                                    _p(nbrs), LAYOUTS.get(layout, layout), _stream(stream), C.byref(self.h)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            load().eh_batch_free(self.h)
+            self.h = None
+
+    def count(self, k, d_counts, stream=None):
+        check(load().eh_batch_count(self.h, k, C.c_void_p(d_counts), _stream(stream)))
+
+    def run(self, d_triangles, d_cliques4, use_graph=True, stream=None):
+        check(load().eh_batch_run(self.h, C.c_void_p(d_triangles), C.c_void_p(d_cliques4), int(use_graph),
+                                  _stream(stream)))
+
+    def tune(self, stream=None):
+        t = Tuning()
+        check(load().eh_batch_tune(self.h, _stream(stream), C.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
+    def matrix_info(self):
+        m = C.c_void_p()
+        check(load().eh_batch_matrix(self.h, C.byref(m)))
+        i = MatrixInfo()
+        check(load().eh_matrix_get_info(m, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in MatrixInfo._fields_}
+
+
+class Server:
+    """Device-resident graphs answering triangle / clique / similar_nodes queries
+    with continuous batching (see eh_server_* in include/eh_gb300.h)."""
+
+    def __init__(self, slots=8, hbm_cap_bytes=150 << 30):
+        cfg = ServerConfig(slots, hbm_cap_bytes)
+        self.h = C.c_void_p()
+        check(load().eh_server_create(C.byref(cfg), C.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            load().eh_server_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def add_graph(self, offsets, nbrs, layout="hybrid"):
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        nbrs = np.ascontiguousarray(nbrs, np.uint32)
+        gid = C.c_uint32()
+        check(load().eh_server_add_graph(self.h, len(offsets) - 1, _p(offsets), _p(nbrs),
+                                         LAYOUTS.get(layout, layout), C.byref(gid)))
+        return gid.value
+
+    def submit(self, graph_id, kind, param=0):
+        t = C.c_uint64()
+        check(load().eh_server_submit(self.h, graph_id, kind, param, C.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout_ms=60000):
+        r = QueryResult()
+        check(load().eh_server_wait(self.h, ticket, timeout_ms, C.byref(r)))
+        return {k: getattr(r, k) for k, _ in QueryResult._fields_}
+
+    def run_alone(self, graph_id, kind, param=0):
+        c = C.c_uint64()
+        check(load().eh_server_run_alone(self.h, graph_id, kind, param, C.byref(c)))
+        return c.value
+
+    def stats(self):
+        c = ServerCounters()
+        check(load().eh_server_stats(self.h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in ServerCounters._fields_}
+
+
+def concat_graphs(csrs):
+    """Block-diagonal union of (offsets, nbrs) pairs -> (graph_rows, offsets, nbrs)."""
+    rows = [len(o) - 1 for o, _ in csrs]
+    graph_rows = np.zeros(len(csrs) + 1, np.uint64)
+    graph_rows[1:] = np.cumsum(rows)
+    offs, nbs = [np.zeros(1, np.uint64)], []
+    base_e = 0
+    for g, (o, b) in enumerate(csrs):
+        offs.append(o[1:].astype(np.uint64) + np.uint64(base_e))
+        nbs.append(b.astype(np.uint32) + np.uint32(graph_rows[g]))
+        base_e += len(b)
+    return graph_rows, np.concatenate(offs), (np.concatenate(nbs) if nbs else np.zeros(0, np.uint32))
 
 
 def graph(kind, seed, **kw):

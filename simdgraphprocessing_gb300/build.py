@@ -65,7 +65,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         jobs.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
-                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE, *extra_nvcc,
+                     "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp", "-I", INCLUDE, *extra_nvcc,
                      "-c", src, "-o", obj])
     for src in cpp:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")

@@ -9,46 +9,9 @@
 
 #include "eh_internal.h"
 #include "eh_kernels.cuh"
+#include "eh_matrix.cuh"
 
 namespace eh {
-
-struct Plan {
-  bool ready = false;
-  uint32_t* order = nullptr;  // rows with card >= 2, descending card
-  uint32_t n_order = 0, n_heavy = 0, n_giant = 0;
-  uint2* units = nullptr;     // heavy units (order position, part)
-  uint32_t n_units = 0;
-  uint32_t* giant_lists = nullptr;
-  unsigned long long* giant_off = nullptr;
-  std::vector<uint32_t> starts;  // bin starts: rows with card > x are order[0, starts[65535 - x])
-  // rows in the plan with card > x (x < 65535)
-  uint32_t above(uint32_t x) const { return starts.empty() ? 0 : starts[65535 - x]; }
-  // largest card <= x present in the plan (0 if none)
-  uint32_t largest_at_most(uint32_t x) const {
-    if (starts.empty()) return 0;
-    for (uint32_t b = 65535 - x; b < 65535; b++)
-      if (starts[b + 1] > starts[b]) return 65535 - b;
-    return 0;
-  }
-};
-
-struct Matrix {
-  int device = 0;
-  uint64_t n = 0;
-  int layout = 0, selection = 0;
-  RowDesc* desc = nullptr;
-  uint4* arena = nullptr;
-  uint64_t arena_units = 0;
-  BuildTotals tot{};
-  Plan plan;
-  uint32_t* counters = nullptr;
-  unsigned long long* result = nullptr;
-  int grid = 0;
-  int64_t vstar = -1;
-  uint64_t device_bytes = 0;
-  uint32_t* clique_scratch = nullptr;  // global slots for the largest clique pivots
-  uint64_t clique_scratch_words = 0;
-};
 
 static eh_status cuda_fail(cudaError_t e, const char* what) {
   return set_error(EH_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
@@ -73,7 +36,7 @@ static uint64_t flattened_bytes(int layout, const RowDesc& d) {
   return inner + (is_hybrid(layout) ? 8 : 0);
 }
 
-static eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask,
+eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask,
                               int sel, int layout, cudaStream_t st, Matrix** out) {
   EH_CHECK_ARG(out != nullptr, "out is NULL");
   EH_CHECK_ARG(valid_layout(layout), "unknown layout %d", layout);
@@ -158,95 +121,119 @@ static eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t*
   return EH_OK;
 }
 
-static eh_status ensure_plan(Matrix* m, cudaStream_t st) {
+// (Re)builds the heavy-unit list of the plan for (light_max, unit_span).
+eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaStream_t st) {
   Plan& p = m->plan;
-  if (p.ready) return EH_OK;
-  uint32_t* hist = nullptr;
-  uint32_t* cursor = nullptr;
-  const uint64_t nn = m->n ? m->n : 1;
-  CU(cudaMalloc((void**)&p.order, nn * sizeof(uint32_t)), "plan order allocation");
-  m->device_bytes += nn * sizeof(uint32_t);
-  CU(cudaMallocAsync((void**)&hist, (65536 + scan_tmp_words(65536)) * sizeof(uint32_t), st), "plan scratch");
-  CU(cudaMallocAsync((void**)&cursor, 65536 * sizeof(uint32_t), st), "plan scratch");
-  CU(launch_plan(m->n, m->desc, 2, hist, p.order, cursor, st), "plan kernels");
-  std::vector<uint32_t> starts(65536);
-  uint32_t total = 0;
-  CU(cudaMemcpyAsync(starts.data(), hist, 65536 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "plan copy");
-  CU(cudaMemcpyAsync(&total, cursor + 65535, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "plan copy");
-  CU(cudaStreamSynchronize(st), "plan");
-  p.n_order = m->n ? total : 0;
-  p.starts = starts;
-  p.n_heavy = m->n ? starts[65535 - kLightMax] : 0;
-  p.n_giant = m->n ? starts[65535 - kCtaListCap] : 0;
-  // Heavy units.
+  if (p.units && p.light_max == light_max && p.unit_span == unit_span) return EH_OK;
+  const uint32_t n_heavy = p.above(light_max);
   uint32_t* cnt = nullptr;
   uint32_t* start = nullptr;
   uint32_t* tmp = nullptr;
-  const uint32_t nh = p.n_heavy ? p.n_heavy : 1;
+  const uint32_t nh = n_heavy ? n_heavy : 1;
   CU(cudaMallocAsync((void**)&cnt, nh * sizeof(uint32_t), st), "unit scratch");
   CU(cudaMallocAsync((void**)&start, nh * sizeof(uint32_t), st), "unit scratch");
   CU(cudaMallocAsync((void**)&tmp, scan_tmp_words(nh) * sizeof(uint32_t), st), "unit scratch");
-  CU(launch_pivot_units(m->desc, p.order, p.n_heavy, cnt, st), "unit count");
-  p.n_units = 0;
-  if (p.n_heavy) {
-    CU(exclusive_scan_u32(cnt, p.n_heavy, start, tmp, st), "unit scan");
+  CU(launch_pivot_units(m->desc, p.order, n_heavy, unit_span, cnt, st), "unit count");
+  uint32_t n_units = 0;
+  if (n_heavy) {
+    CU(exclusive_scan_u32(cnt, n_heavy, start, tmp, st), "unit scan");
     uint32_t last_start = 0, last_cnt = 0;
-    CU(cudaMemcpyAsync(&last_start, start + p.n_heavy - 1, 4, cudaMemcpyDeviceToHost, st), "unit copy");
-    CU(cudaMemcpyAsync(&last_cnt, cnt + p.n_heavy - 1, 4, cudaMemcpyDeviceToHost, st), "unit copy");
+    CU(cudaMemcpyAsync(&last_start, start + n_heavy - 1, 4, cudaMemcpyDeviceToHost, st), "unit copy");
+    CU(cudaMemcpyAsync(&last_cnt, cnt + n_heavy - 1, 4, cudaMemcpyDeviceToHost, st), "unit copy");
     CU(cudaStreamSynchronize(st), "units");
-    p.n_units = last_start + last_cnt;
+    n_units = last_start + last_cnt;
   }
-  CU(cudaMalloc((void**)&p.units, (p.n_units ? p.n_units : 1) * sizeof(uint2)), "unit allocation");
-  m->device_bytes += (p.n_units ? p.n_units : 1) * sizeof(uint2);
-  CU(launch_pivot_unit_fill(cnt, start, p.n_heavy, p.units, st), "unit fill");
-  // Giant pivots that are not uint rows get a decoded list.
-  std::vector<uint32_t> grows(p.n_giant);
-  std::vector<unsigned long long> goff(p.n_giant ? p.n_giant : 1, 0);
-  uint64_t gtotal = 0;
-  std::vector<uint32_t> dec_rows;
-  std::vector<unsigned long long> dec_off;
-  if (p.n_giant) {
-    CU(cudaMemcpyAsync(grows.data(), p.order, p.n_giant * sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "giant copy");
-    CU(cudaStreamSynchronize(st), "giant");
-    for (uint32_t u = 0; u < p.n_giant; u++) {
-      RowDesc d;
-      CU(cudaMemcpy(&d, m->desc + grows[u], sizeof(RowDesc), cudaMemcpyDeviceToHost), "giant desc");
-      if (desc_type(d) != TY_UINT) {
-        goff[u] = gtotal;
-        dec_rows.push_back(grows[u]);
-        dec_off.push_back(gtotal);
-        gtotal += d.card;
-      }
+  if (!p.units || p.units_cap < (uint64_t)n_units) {
+    CU(cudaStreamSynchronize(st), "units");
+    if (p.units) {
+      cudaFree(p.units);
+      m->device_bytes -= p.units_cap * sizeof(uint2);
     }
+    p.units_cap = n_units ? n_units : 1;
+    CU(cudaMalloc((void**)&p.units, p.units_cap * sizeof(uint2)), "unit allocation");
+    m->device_bytes += p.units_cap * sizeof(uint2);
   }
-  CU(cudaMalloc((void**)&p.giant_off, goff.size() * sizeof(unsigned long long)), "giant allocation");
-  CU(cudaMalloc((void**)&p.giant_lists, (gtotal ? gtotal : 1) * sizeof(uint32_t)), "giant allocation");
-  m->device_bytes += goff.size() * 8 + (gtotal ? gtotal : 1) * 4;
-  CU(cudaMemcpyAsync(p.giant_off, goff.data(), goff.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, st),
-     "giant copy");
-  if (!dec_rows.empty()) {
-    uint32_t* d_rows = nullptr;
-    unsigned long long* d_off = nullptr;
-    CU(cudaMallocAsync((void**)&d_rows, dec_rows.size() * 4, st), "giant scratch");
-    CU(cudaMallocAsync((void**)&d_off, dec_off.size() * 8, st), "giant scratch");
-    CU(cudaMemcpyAsync(d_rows, dec_rows.data(), dec_rows.size() * 4, cudaMemcpyHostToDevice, st), "giant copy");
-    CU(cudaMemcpyAsync(d_off, dec_off.data(), dec_off.size() * 8, cudaMemcpyHostToDevice, st), "giant copy");
-    CU(launch_decode_rows(m->desc, m->arena, d_rows, d_off, (uint32_t)dec_rows.size(), p.giant_lists, st),
-       "giant decode");
-    cudaFreeAsync(d_rows, st);
-    cudaFreeAsync(d_off, st);
-  }
+  CU(launch_pivot_unit_fill(cnt, start, n_heavy, p.units, st), "unit fill");
   cudaFreeAsync(cnt, st);
   cudaFreeAsync(start, st);
   cudaFreeAsync(tmp, st);
-  cudaFreeAsync(hist, st);
-  cudaFreeAsync(cursor, st);
-  CU(cudaStreamSynchronize(st), "plan build");
-  p.ready = true;
+  CU(cudaStreamSynchronize(st), "unit build");
+  p.n_heavy = n_heavy;
+  p.n_units = n_units;
+  p.light_max = light_max;
+  p.unit_span = unit_span;
   return EH_OK;
 }
 
-static PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
+// Row order (descending card) and decoded copies of the giant non-uint pivots,
+// then the heavy units for the matrix's current work shape.
+eh_status ensure_plan(Matrix* m, cudaStream_t st) {
+  Plan& p = m->plan;
+  if (!p.ready) {
+    uint32_t* hist = nullptr;
+    uint32_t* cursor = nullptr;
+    const uint64_t nn = m->n ? m->n : 1;
+    CU(cudaMalloc((void**)&p.order, nn * sizeof(uint32_t)), "plan order allocation");
+    m->device_bytes += nn * sizeof(uint32_t);
+    CU(cudaMallocAsync((void**)&hist, (65536 + scan_tmp_words(65536)) * sizeof(uint32_t), st), "plan scratch");
+    CU(cudaMallocAsync((void**)&cursor, 65536 * sizeof(uint32_t), st), "plan scratch");
+    CU(launch_plan(m->n, m->desc, 2, hist, p.order, cursor, st), "plan kernels");
+    std::vector<uint32_t> starts(65536);
+    uint32_t total = 0;
+    CU(cudaMemcpyAsync(starts.data(), hist, 65536 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "plan copy");
+    CU(cudaMemcpyAsync(&total, cursor + 65535, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "plan copy");
+    CU(cudaStreamSynchronize(st), "plan");
+    cudaFreeAsync(hist, st);
+    cudaFreeAsync(cursor, st);
+    p.n_order = m->n ? total : 0;
+    if (m->n) p.starts = starts;
+    p.n_giant = p.above(kCtaListCap);
+    // Giant pivots that are not uint rows get a decoded list.
+    std::vector<uint32_t> grows(p.n_giant);
+    std::vector<unsigned long long> goff(p.n_giant ? p.n_giant : 1, 0);
+    uint64_t gtotal = 0;
+    std::vector<uint32_t> dec_rows;
+    std::vector<unsigned long long> dec_off;
+    if (p.n_giant) {
+      CU(cudaMemcpyAsync(grows.data(), p.order, p.n_giant * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+         "giant copy");
+      CU(cudaStreamSynchronize(st), "giant");
+      for (uint32_t u = 0; u < p.n_giant; u++) {
+        RowDesc d;
+        CU(cudaMemcpy(&d, m->desc + grows[u], sizeof(RowDesc), cudaMemcpyDeviceToHost), "giant desc");
+        if (desc_type(d) != TY_UINT) {
+          goff[u] = gtotal;
+          dec_rows.push_back(grows[u]);
+          dec_off.push_back(gtotal);
+          gtotal += d.card;
+        }
+      }
+    }
+    CU(cudaMalloc((void**)&p.giant_off, goff.size() * sizeof(unsigned long long)), "giant allocation");
+    CU(cudaMalloc((void**)&p.giant_lists, (gtotal ? gtotal : 1) * sizeof(uint32_t)), "giant allocation");
+    m->device_bytes += goff.size() * 8 + (gtotal ? gtotal : 1) * 4;
+    CU(cudaMemcpyAsync(p.giant_off, goff.data(), goff.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                       st),
+       "giant copy");
+    if (!dec_rows.empty()) {
+      uint32_t* d_rows = nullptr;
+      unsigned long long* d_off = nullptr;
+      CU(cudaMallocAsync((void**)&d_rows, dec_rows.size() * 4, st), "giant scratch");
+      CU(cudaMallocAsync((void**)&d_off, dec_off.size() * 8, st), "giant scratch");
+      CU(cudaMemcpyAsync(d_rows, dec_rows.data(), dec_rows.size() * 4, cudaMemcpyHostToDevice, st), "giant copy");
+      CU(cudaMemcpyAsync(d_off, dec_off.data(), dec_off.size() * 8, cudaMemcpyHostToDevice, st), "giant copy");
+      CU(launch_decode_rows(m->desc, m->arena, d_rows, d_off, (uint32_t)dec_rows.size(), p.giant_lists, st),
+         "giant decode");
+      cudaFreeAsync(d_rows, st);
+      cudaFreeAsync(d_off, st);
+    }
+    CU(cudaStreamSynchronize(st), "plan build");
+    p.ready = true;
+  }
+  return ensure_units(m, m->light_max, m->unit_span, st);
+}
+
+PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
   PivotArgs a;
   a.desc = m->desc;
   a.arena = m->arena;
@@ -258,6 +245,9 @@ static PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
   a.giant_off = m->plan.giant_off;
   a.counters = m->counters;
   a.out = out;
+  a.unit_span = m->plan.unit_span;
+  a.graph_rows = nullptr;
+  a.num_graphs = 0;
   return a;
 }
 
@@ -265,6 +255,80 @@ static eh_status finish_sync(Matrix* m, unsigned long long* d_res, uint64_t* cou
   (void)m;
   CU(cudaMemcpyAsync(count, d_res, sizeof(uint64_t), cudaMemcpyDeviceToHost, st), "result copy");
   CU(cudaStreamSynchronize(st), "count");
+  return EH_OK;
+}
+
+eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const uint32_t* graph_rows,
+                         uint32_t num_graphs, cudaStream_t st, Workspace* ws) {
+  Workspace own;
+  if (!ws) {
+    own.counters = m->counters;
+    own.clique_scratch = m->clique_scratch;
+    own.clique_scratch_words = m->clique_scratch_words;
+  }
+  Workspace& w = ws ? *ws : own;
+  if (m->selection != EH_SELECT_LOWER)
+    return set_error(EH_ERR_UNSUPPORTED, "clique counting needs a matrix built with EH_SELECT_LOWER");
+  if (k > kCliqueMaxK)
+    return set_error(EH_ERR_UNSUPPORTED, "clique size %u above the supported maximum %u", k, kCliqueMaxK);
+  CU(cudaMemsetAsync(out, 0, sizeof(uint64_t) * (graph_rows ? num_graphs : 1), st), "memset");
+  // The reference's recursion only returns a count at depth n >= 3 (apps/n_clique.cpp:41-43);
+  // for n < 3 it never reaches that depth and the count stays 0.
+  if (k < 3) return EH_OK;
+  eh_status s = ensure_plan(m, st);
+  if (s != EH_OK) return s;
+  const Plan& p = m->plan;
+  const uint32_t nG = p.above(kCliqueSmemMax);
+  const uint32_t nB = p.above(32);
+  const uint32_t nL = p.above(k - 2);
+  CliqueArgs a{m->desc, m->arena, p.order, k, out, graph_rows, num_graphs};
+  CU(cudaMemsetAsync(w.counters, 0, 8 * sizeof(uint32_t), st), "memset");
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
+  if (nG > 0) {
+    const uint32_t cmax = (uint32_t)m->tot.max_card;
+    int grid = (int)std::min<uint64_t>(nG, 2ull * sms);
+    const uint64_t slot = clique_slot_words(cmax, k);
+    if (slot * grid > w.clique_scratch_words) {
+      if (ws) {  // a caller's workspace is never grown here: use the slots it has
+        grid = (int)std::min<uint64_t>(grid, w.clique_scratch_words / slot);
+        if (grid < 1) return set_error(EH_ERR_OUT_OF_MEMORY, "workspace too small for a %u-entry pivot", cmax);
+      } else {
+        cudaStreamSynchronize(st);
+        cudaFree(m->clique_scratch);
+        m->clique_scratch = nullptr;
+        m->clique_scratch_words = 0;
+        CU(cudaMalloc((void**)&m->clique_scratch, slot * grid * 4), "clique scratch allocation");
+        m->clique_scratch_words = slot * grid;
+        w.clique_scratch = m->clique_scratch;
+        w.clique_scratch_words = m->clique_scratch_words;
+      }
+    }
+    CU(launch_clique_cta(a, 0, nG, w.counters + 2, cmax, w.clique_scratch, grid, st), "clique kernel (global)");
+  }
+  if (nB > nG) {
+    const uint32_t cmax = p.largest_at_most(kCliqueSmemMax);
+    const int grid = (int)std::min<uint64_t>(nB - nG, 4ull * sms);
+    CU(launch_clique_cta(a, nG, nB, w.counters + 3, cmax, nullptr, grid, st), "clique kernel (shared)");
+  }
+  if (nL > nB) {
+    const int grid = (int)std::min<uint64_t>((nL - nB + 63) / 64, 8ull * sms);
+    CU(launch_clique_light(a, nB, nL, w.counters + 4, grid > 0 ? grid : 1, st), "clique kernel (warp)");
+  }
+  return EH_OK;
+}
+
+eh_status launch_triangle_count(Matrix* m, unsigned long long* out, const uint32_t* graph_rows, uint32_t num_graphs,
+                                cudaStream_t st, Workspace* ws) {
+  if (m->selection != EH_SELECT_LOWER)
+    return set_error(EH_ERR_UNSUPPORTED, "triangle counting needs a matrix built with EH_SELECT_LOWER");
+  eh_status s = ensure_plan(m, st);
+  if (s != EH_OK) return s;
+  PivotArgs a = pivot_args(m, out);
+  if (ws) a.counters = ws->counters;
+  a.graph_rows = graph_rows;
+  a.num_graphs = num_graphs;
+  CU(launch_triangles(a, m->plan.units, m->plan.n_units, m->grid, st), "triangle kernel");
   return EH_OK;
 }
 
@@ -467,14 +531,7 @@ void eh_matrix_free(eh_matrix_t mh) {
 eh_status eh_count_triangles_async(eh_matrix_t mh, uint64_t* d_count, void* stream) {
   CHECK_MATRIX(mh);
   EH_CHECK_ARG(d_count, "d_count is NULL");
-  Matrix* m = MX(mh);
-  if (m->selection != EH_SELECT_LOWER)
-    return set_error(EH_ERR_UNSUPPORTED, "triangle counting needs a matrix built with EH_SELECT_LOWER");
-  eh_status s = eh::ensure_plan(m, ST(stream));
-  if (s != EH_OK) return s;
-  eh::PivotArgs a = eh::pivot_args(m, reinterpret_cast<unsigned long long*>(d_count));
-  CU(eh::launch_triangles(a, m->plan.units, m->plan.n_units, m->grid, ST(stream)), "triangle kernel");
-  return EH_OK;
+  return eh::launch_triangle_count(MX(mh), reinterpret_cast<unsigned long long*>(d_count), nullptr, 0, ST(stream));
 }
 
 eh_status eh_count_triangles(eh_matrix_t mh, uint64_t* count, void* stream) {
@@ -537,50 +594,7 @@ eh_status eh_intersect_rows(eh_matrix_t mh, const uint32_t* d_a, const uint32_t*
 eh_status eh_count_cliques_async(eh_matrix_t mh, uint32_t k, uint64_t* d_count, void* stream) {
   CHECK_MATRIX(mh);
   EH_CHECK_ARG(d_count, "d_count is NULL");
-  Matrix* m = MX(mh);
-  cudaStream_t st = ST(stream);
-  if (m->selection != EH_SELECT_LOWER)
-    return set_error(EH_ERR_UNSUPPORTED, "clique counting needs a matrix built with EH_SELECT_LOWER");
-  if (k > eh::kCliqueMaxK)
-    return set_error(EH_ERR_UNSUPPORTED, "clique size %u above the supported maximum %u", k, eh::kCliqueMaxK);
-  CU(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), st), "memset");
-  // The reference's recursion only returns a count at depth n >= 3 (apps/n_clique.cpp:41-43);
-  // for n < 3 it never reaches that depth and the count stays 0.
-  if (k < 3) return EH_OK;
-  eh_status s = eh::ensure_plan(m, st);
-  if (s != EH_OK) return s;
-  const eh::Plan& p = m->plan;
-  const uint32_t nG = p.above(eh::kCliqueSmemMax);
-  const uint32_t nB = p.above(32);
-  const uint32_t nL = p.above(k - 2);
-  eh::CliqueArgs a{m->desc, m->arena, p.order, k, reinterpret_cast<unsigned long long*>(d_count)};
-  CU(cudaMemsetAsync(m->counters, 0, 8 * sizeof(uint32_t), st), "memset");
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
-  if (nG > 0) {
-    const uint32_t cmax = (uint32_t)m->tot.max_card;
-    const int grid = (int)std::min<uint64_t>(nG, 2ull * sms);
-    const uint64_t words = eh::clique_slot_words(cmax, k) * grid;
-    if (words > m->clique_scratch_words) {
-      cudaStreamSynchronize(st);
-      cudaFree(m->clique_scratch);
-      m->clique_scratch = nullptr;
-      m->clique_scratch_words = 0;
-      CU(cudaMalloc((void**)&m->clique_scratch, words * 4), "clique scratch allocation");
-      m->clique_scratch_words = words;
-    }
-    CU(eh::launch_clique_cta(a, 0, nG, m->counters + 2, cmax, m->clique_scratch, grid, st), "clique kernel (global)");
-  }
-  if (nB > nG) {
-    const uint32_t cmax = p.largest_at_most(eh::kCliqueSmemMax);
-    const int grid = (int)std::min<uint64_t>(nB - nG, 4ull * sms);
-    CU(eh::launch_clique_cta(a, nG, nB, m->counters + 3, cmax, nullptr, grid, st), "clique kernel (shared)");
-  }
-  if (nL > nB) {
-    const int grid = (int)std::min<uint64_t>((nL - nB + 63) / 64, 8ull * sms);
-    CU(eh::launch_clique_light(a, nB, nL, m->counters + 4, grid > 0 ? grid : 1, st), "clique kernel (warp)");
-  }
-  return EH_OK;
+  return eh::launch_cliques(MX(mh), k, reinterpret_cast<unsigned long long*>(d_count), nullptr, 0, ST(stream));
 }
 
 eh_status eh_count_cliques(eh_matrix_t mh, uint32_t k, uint64_t* count, void* stream) {

@@ -18,6 +18,7 @@
 // one-word masks (|A_i| <= 32); one CTA per pivot with masks in shared memory
 // (|A_i| <= kCliqueSmemMax); one CTA per pivot with masks in a global scratch
 // slot (larger pivots).
+#include <atomic>
 #include <cstdint>
 
 #include "eh_kernels.cuh"
@@ -47,8 +48,10 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
     if (base >= pos_end) break;
     const uint32_t end = min(pos_end, base + 8u);
     for (uint32_t p = base; p < end; p++) {
-      const RowView A = load_view(a.desc, a.arena, a.order[p]);
+      const uint32_t row = a.order[p];
+      const RowView A = load_view(a.desc, a.arena, row);
       const uint32_t c = A.card;
+      const unsigned long long acc_before = acc;
       warp_decode(A, list, lane);
       mask[lane] = 0;
       __syncwarp();
@@ -99,6 +102,11 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
           }
         }
       }
+      if (a.graph_rows) {  // batch: this pivot's cliques go to its graph
+        const unsigned long long pc = warp_sum_u64(acc - acc_before);
+        acc = acc_before;
+        if (lane == 0 && pc) atomicAdd(&a.out[graph_of(a.graph_rows, a.num_graphs, row)], pc);
+      }
       __syncwarp();
     }
   }
@@ -128,8 +136,10 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
     __syncthreads();
     const uint32_t unit = s_unit;
     if (unit >= pos_end) break;
-    const RowView A = load_view(a.desc, a.arena, a.order[unit]);
+    const uint32_t row = a.order[unit];
+    const RowView A = load_view(a.desc, a.arena, row);
     const uint32_t c = A.card;
+    const unsigned long long acc_before = acc;
     cta_decode<kCtaThreads>(A, list, s_scan);
     for (uint64_t x = threadIdx.x; x < (uint64_t)c * W; x += kCtaThreads) masks[x] = 0;
     __syncthreads();
@@ -220,6 +230,11 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
         }
       }
     }
+    if (a.graph_rows) {  // batch: each warp's share of this pivot goes to its graph
+      const unsigned long long pc = warp_sum_u64(acc - acc_before);
+      acc = acc_before;
+      if (lane == 0 && pc) atomicAdd(&a.out[graph_of(a.graph_rows, a.num_graphs, row)], pc);
+    }
     __syncthreads();
   }
   acc = warp_sum_u64(acc);
@@ -249,8 +264,19 @@ cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t 
     k_clique_cta<true><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch, slot);
   } else {
     const size_t bytes = slot * 4;
-    cudaError_t e = cudaFuncSetAttribute(k_clique_cta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return e;
+    // Raise the kernel's dynamic shared-memory limit only when a launch needs more
+    // than any before it (so replays of captured launches never call this).
+    static std::atomic<int> set_bytes[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if ((int)bytes > set_bytes[dev].load()) {
+      cudaError_t e = cudaFuncSetAttribute(k_clique_cta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      if (e != cudaSuccess) return e;
+      int prev = set_bytes[dev].load();
+      while ((int)bytes > prev && !set_bytes[dev].compare_exchange_weak(prev, (int)bytes)) {
+      }
+    }
     k_clique_cta<false><<<grid, kCtaThreads, bytes, st>>>(a, pos_begin, pos_end, counter, cmax, W, nullptr, slot);
   }
   return cudaGetLastError();

@@ -11,7 +11,7 @@
 // One persistent kernel does both.  Work comes in two tiers, both handed out
 // dynamically with an atomic counter (the GPU form of par_for_range's block
 // stealing, src/common.hpp:214-276):
-//  * heavy pivots (|A_i| > kLightMax) are split into units of kUnitSpan values
+//  * heavy pivots (|A_i| > light_max) are split into units of unit_span values
 //    of e; a CTA stages the pivot's decoded list (and, for bitset rows, its
 //    words) in shared memory and its warps take one j each.  Per pair the warp
 //    picks the cheapest of: AND of overlapping bitset words + popc (bitset ∩
@@ -33,7 +33,6 @@ namespace eh {
 namespace {
 
 constexpr int NWARPS = kCtaThreads / 32;
-constexpr uint32_t kUnitSpan = 128;   // values of e per heavy unit
 constexpr uint32_t kLightChunk = 16;  // light pivots per atomic grab
 
 struct __align__(16) PivotSmem {
@@ -119,13 +118,19 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
     }
     __syncthreads();
     const uint32_t c = A.card;
-    const uint32_t e0 = 1 + uu.y * kUnitSpan;
-    const uint32_t e1 = min(c, e0 + kUnitSpan);
+    const uint32_t e0 = 1 + uu.y * a.unit_span;
+    const uint32_t e1 = min(c, e0 + a.unit_span);
+    unsigned long long uacc = 0;
     for (uint32_t e = e0 + warp; e < e1; e += NWARPS) {
       const uint32_t j = L[e];
       const RowView B = load_view(a.desc, a.arena, j);
       const uint32_t cnt = pair_count_warp(L, e, A, B, j, lane);
-      if (lane == 0) acc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+      if (lane == 0) uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+    }
+    if (a.graph_rows) {  // batch: this unit's count goes to its graph
+      if (lane == 0 && uacc) atomicAdd(&a.out[graph_of(a.graph_rows, a.num_graphs, i)], uacc);
+    } else {
+      acc += uacc;
     }
     __syncthreads();
   }
@@ -140,7 +145,8 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
     if (base >= n_light) break;
     const uint32_t end = min(n_light, base + kLightChunk);
     for (uint32_t k = base; k < end; k++) {
-      const RowView A = load_view(a.desc, a.arena, a.order[a.n_heavy + k]);
+      const uint32_t i = a.order[a.n_heavy + k];
+      const RowView A = load_view(a.desc, a.arena, i);
       const uint32_t c = A.card;
       warp_decode(A, list, lane);
       const uint32_t pairs = c * (c - 1) / 2;
@@ -154,7 +160,13 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
         t += 32;
         while (t >= e && e < c) { t -= e; e++; }
       }
-      acc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+      unsigned long long pc = LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+      if (a.graph_rows) {  // batch: one atomic per pivot into its graph's count
+        pc = warp_sum_u64(pc);
+        if (lane == 0 && pc) atomicAdd(&a.out[graph_of(a.graph_rows, a.num_graphs, i)], pc);
+      } else {
+        acc += pc;
+      }
       __syncwarp();
     }
   }
@@ -167,17 +179,17 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
   if (threadIdx.x == 0) {
     unsigned long long tot = 0;
     for (int w = 0; w < NWARPS; w++) tot += s_red[w];
-    if (tot) atomicAdd(a.out, tot);
+    if (tot && !a.graph_rows) atomicAdd(a.out, tot);
   }
 }
 
-// Heavy units: for order position u < n_heavy, ceil((card-1)/kUnitSpan) units (u, part).
+// Heavy units: for order position u < n_heavy, ceil((card-1)/span) units (u, part).
 __global__ void k_unit_counts(const RowDesc* __restrict__ desc, const uint32_t* __restrict__ order,
-                              uint32_t n_heavy, uint32_t* __restrict__ cnt) {
+                              uint32_t n_heavy, uint32_t span, uint32_t* __restrict__ cnt) {
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u < n_heavy) {
     const uint32_t c = desc[order[u]].card;
-    cnt[u] = (c - 1 + kUnitSpan - 1) / kUnitSpan;
+    cnt[u] = (c - 1 + span - 1) / span;
   }
 }
 __global__ void k_unit_fill(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ start,
@@ -249,16 +261,16 @@ static cudaError_t launch_pivots(const PivotArgs& a, const uint2* units, uint32_
                                  cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(a.counters, 0, 2 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(a.out, 0, sizeof(unsigned long long), st);
+  e = cudaMemsetAsync(a.out, 0, sizeof(unsigned long long) * (a.graph_rows ? a.num_graphs : 1), st);
   if (e != cudaSuccess) return e;
   k_pivots<LOLLI><<<grid, kCtaThreads, 0, st>>>(a, units, n_units);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pivot_units(const RowDesc* desc, const uint32_t* order, uint32_t n_heavy,
-                               uint32_t* cnt, cudaStream_t st) {
+                               uint32_t unit_span, uint32_t* cnt, cudaStream_t st) {
   if (n_heavy == 0) return cudaSuccess;
-  k_unit_counts<<<(n_heavy + 255) / 256, 256, 0, st>>>(desc, order, n_heavy, cnt);
+  k_unit_counts<<<(n_heavy + 255) / 256, 256, 0, st>>>(desc, order, n_heavy, unit_span, cnt);
   return cudaGetLastError();
 }
 cudaError_t launch_pivot_unit_fill(const uint32_t* cnt, const uint32_t* start, uint32_t n_heavy,

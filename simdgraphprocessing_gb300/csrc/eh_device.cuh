@@ -178,6 +178,17 @@ __device__ inline uint64_t pshort_pair_drop(const RowView& A, const RowView& B, 
   return drop;
 }
 
+// Batch mode: index g of the graph whose rows [graph_rows[g], graph_rows[g+1])
+// hold `row` (graph_rows has num_graphs + 1 ascending entries).
+__device__ __forceinline__ uint32_t graph_of(const uint32_t* graph_rows, uint32_t num_graphs, uint32_t row) {
+  uint32_t lo = 0, hi = num_graphs;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (graph_rows[mid] <= row) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // Layout payload bytes of a row as the algorithmic-bytes formula counts them:
 // uint 4|S|, bitset 8 (words + 1), pshort 2 (|S| + 2 partitions).
 __device__ __forceinline__ uint64_t payload_bytes(const RowView& V) {

@@ -68,21 +68,26 @@ struct PivotArgs {
   const uint32_t* giant_lists;
   const unsigned long long* giant_off;
   uint32_t* counters;      // [0] next heavy unit, [1] next light chunk
-  unsigned long long* out; // result
+  unsigned long long* out; // result; in batch mode out[num_graphs]
+  uint32_t unit_span;      // pivot positions e per heavy unit
+  const uint32_t* graph_rows;  // batch mode: graph g owns rows [graph_rows[g], graph_rows[g+1]); else null
+  uint32_t num_graphs;
 };
 constexpr uint32_t kCtaThreads = 256;
-constexpr uint32_t kLightMax = 96;     // pivots with card <= kLightMax run warp-wide
+constexpr uint32_t kLightMax = 96;     // largest light_max: warp-wide pivots fit a slice of this size
+constexpr uint32_t kDefaultLightMax = 96;
+constexpr uint32_t kDefaultUnitSpan = 128;
 constexpr uint32_t kCtaListCap = 6144; // CTA-staged list capacity (elements)
 constexpr uint32_t kCtaWordCap = 2048; // CTA-staged bitset words capacity
 cudaError_t launch_pivot_units(const RowDesc* desc, const uint32_t* order, uint32_t n_heavy,
-                               uint32_t* cnt, cudaStream_t st);
+                               uint32_t unit_span, uint32_t* cnt, cudaStream_t st);
 cudaError_t launch_pivot_unit_fill(const uint32_t* cnt, const uint32_t* start, uint32_t n_heavy,
                                    uint2* units, cudaStream_t st);
 cudaError_t launch_triangles(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
                              cudaStream_t st);
 cudaError_t launch_lollipops(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
                              cudaStream_t st);
-int pivot_grid(int device);
+int pivot_grid(int device);  // persistent grid: SMs x resident CTAs of the pivot kernel
 cudaError_t launch_similar(uint64_t n, const RowDesc* desc, const uint4* arena, uint32_t vstar,
                            uint32_t threshold, unsigned long long* out, cudaStream_t st);
 cudaError_t launch_intersect_rows(uint64_t n, const RowDesc* desc, const uint4* arena, const uint32_t* a,
@@ -95,7 +100,9 @@ struct CliqueArgs {
   const uint4* arena;
   const uint32_t* order;   // rows sorted by descending card
   uint32_t k;              // clique size, 3 <= k <= kCliqueMaxK
-  unsigned long long* out;
+  unsigned long long* out; // result; in batch mode out[num_graphs]
+  const uint32_t* graph_rows;  // batch mode: graph g owns rows [graph_rows[g], graph_rows[g+1]); else null
+  uint32_t num_graphs;
 };
 constexpr uint32_t kCliqueMaxK = 16;
 constexpr uint32_t kCliqueSmemMax = 1024;  // pivots up to this size keep their masks in shared memory

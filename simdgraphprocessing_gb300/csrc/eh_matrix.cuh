@@ -1,0 +1,82 @@
+// Internal: the device matrix behind eh_matrix_t and its lazily built work plan.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/eh_gb300.h"
+#include "eh_kernels.cuh"
+
+namespace eh {
+
+struct Plan {
+  bool ready = false;
+  uint32_t* order = nullptr;  // rows with card >= 2, descending card
+  uint32_t n_order = 0, n_giant = 0;
+  uint32_t* giant_lists = nullptr;
+  unsigned long long* giant_off = nullptr;
+  std::vector<uint32_t> starts;  // bin starts: rows with card > x are order[0, starts[65535 - x])
+  // Heavy units for the current (light_max, unit_span).
+  uint32_t light_max = 0, unit_span = 0;
+  uint32_t n_heavy = 0;           // order[0, n_heavy) have card > light_max
+  uint2* units = nullptr;         // (order position, part)
+  uint32_t n_units = 0;
+  uint64_t units_cap = 0;
+  // rows in the plan with card > x (x < 65535)
+  uint32_t above(uint32_t x) const { return starts.empty() ? 0 : starts[65535 - x]; }
+  // largest card <= x present in the plan (0 if none)
+  uint32_t largest_at_most(uint32_t x) const {
+    if (starts.empty()) return 0;
+    for (uint32_t b = 65535 - x; b < 65535; b++)
+      if (starts[b + 1] > starts[b]) return 65535 - b;
+    return 0;
+  }
+};
+
+// Per-launch scratch: work-queue counters and the clique kernel's global slots.
+// A matrix has its own; concurrent launches on one matrix (the serving loop)
+// each bring theirs.
+struct Workspace {
+  uint32_t* counters = nullptr;        // >= 8 words
+  uint32_t* clique_scratch = nullptr;
+  uint64_t clique_scratch_words = 0;
+};
+
+struct Matrix {
+  int device = 0;
+  uint64_t n = 0;
+  int layout = 0, selection = 0;
+  RowDesc* desc = nullptr;
+  uint4* arena = nullptr;
+  uint64_t arena_units = 0;
+  BuildTotals tot{};
+  Plan plan;
+  uint32_t* counters = nullptr;
+  unsigned long long* result = nullptr;
+  int grid = 0;
+  int64_t vstar = -1;
+  uint64_t device_bytes = 0;
+  uint32_t* clique_scratch = nullptr;  // global slots for the largest clique pivots
+  uint64_t clique_scratch_words = 0;
+  // Work-shape parameters of the pivot kernel (set by the autotuner).
+  uint32_t light_max = kDefaultLightMax;
+  uint32_t unit_span = kDefaultUnitSpan;
+};
+
+// eh_capi.cu
+eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask, int sel,
+                       int layout, cudaStream_t st, Matrix** out);
+eh_status ensure_plan(Matrix* m, cudaStream_t st);
+eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaStream_t st);
+PivotArgs pivot_args(Matrix* m, unsigned long long* out);
+// Count launches; graph_rows / num_graphs != null selects per-graph outputs
+// out[num_graphs].  ws == null uses the matrix's own workspace.  The plan must
+// already exist when ws != null (launches with a workspace never allocate it).
+eh_status launch_triangle_count(Matrix* m, unsigned long long* out, const uint32_t* graph_rows, uint32_t num_graphs,
+                                cudaStream_t st, Workspace* ws = nullptr);
+eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const uint32_t* graph_rows,
+                         uint32_t num_graphs, cudaStream_t st, Workspace* ws = nullptr);
+
+}  // namespace eh
