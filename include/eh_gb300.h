@@ -169,6 +169,20 @@ eh_status eh_count_triangles_async(eh_matrix_t m, uint64_t* d_count, void* strea
 /* n_clique<T,R>::run / apply_function (apps/n_clique.cpp:30-101), k >= 3. */
 eh_status eh_count_cliques(eh_matrix_t m, uint32_t k, uint64_t* count, void* stream);
 eh_status eh_count_cliques_async(eh_matrix_t m, uint32_t k, uint64_t* d_count, void* stream);
+/* No counterpart in the reference.  The same count as eh_count_cliques_async,
+ * for callers that may not allocate device memory when they count: a serving
+ * loop that reserves its whole device-memory budget at start-up and must not
+ * grow its footprint or meet an allocation failure mid-request, or a host
+ * framework that owns every device allocation (cudaFree also synchronizes the
+ * device).  Nothing is allocated: the largest pivots' scratch slots and the
+ * work counters come from one fixed 16 MiB array in device memory, held by
+ * every GPU that loads the library until exit; a pivot needing a larger slot is
+ * rejected with EH_ERR_UNSUPPORTED.  The matrix must already have its work plan
+ * (made by its first eh_count_* call), else EH_ERR_INVALID_ARGUMENT.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress) and
+ * should come before any stream capture.  All calls share the array: calls
+ * whose kernels overlap on the GPU race. */
+eh_status eh_count_cliques_noalloc(eh_matrix_t m, uint32_t k, uint64_t* d_count, void* stream);
 /* undirected_lollipop_counting<T,R>::run (apps/undirected_lollipop_counting.cpp:27-77).
  * Matrix built with EH_SELECT_ALL. */
 eh_status eh_count_lollipops(eh_matrix_t m, uint64_t* count, void* stream);
