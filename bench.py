@@ -128,6 +128,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, device=None):
+    """Max of a float over all ranks of the default process group (identity when
+    torch.distributed is not initialised).  Works with nccl (device tensor) and
+    gloo (host tensor)."""
+    import torch
+    import torch.distributed as tdist
+    if not (tdist.is_available() and tdist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate(units_per_rank, ms_per_rank, world, device=None):
+    """Whole-job throughput of replicas: every rank processed units_per_rank units;
+    the job takes as long as the slowest rank."""
+    ms = max_over_ranks(ms_per_rank, device)
+    return world * units_per_rank / (ms / 1e3), ms
+
+
 def make_graph(a):
     import simdgraphprocessing_gb300 as eh
     g = eh.graph("rmat", a.seed, scale=a.scale, edges=a.edge_factor << a.scale)
@@ -217,6 +237,7 @@ def run_ours(a, rank, world, local_rank):
     stream = torch.cuda.current_stream()
     st = eh._stream(stream)
     m = eh.Matrix.build(off, nbr, "lower", a.layout, stream=stream)
+    shape = m.tune(stream=stream) if not a.profile else None  # autotuned work shape (cached for later builds)
     info = m.info()
     pruned = info["cardinality"]
     btc = m.triangle_bytes()
@@ -259,13 +280,7 @@ def run_ours(a, rank, world, local_rank):
     count = int(out.item())
     if count != count_ref:
         raise SystemExit("nondeterministic count: %d vs %d" % (count, count_ref))
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    else:
-        ms_max = ms
-    value = world * pruned / (ms_max / 1e3)
+    value, ms_max = aggregate(pruned, ms, world, "cuda")
 
     # End to end through the C ABI from pinned host buffers.
     e2e = None
@@ -293,12 +308,8 @@ def run_ours(a, rank, world, local_rank):
                 e2e_times.append(dt)
         for h in keep:
             L.eh_matrix_free(h)
-        e2e_ms = 1e3 * statistics.mean(e2e_times)
-        if dist:
-            t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": world * pruned / (e2e_ms / 1e3), "unit": "edges/s",
+        e2e_value, e2e_ms = aggregate(pruned, 1e3 * statistics.mean(e2e_times), world, "cuda")
+        e2e = {"value": e2e_value, "unit": "edges/s",
                "h2d_bytes_per_step": int(off.nbytes + nbr.nbytes), "d2h_bytes_per_step": 8,
                "ms_per_step": e2e_ms, "steps": len(e2e_times),
                "includes": "pinned H2D of the full symmetric CSR, device select/optimize/encode/plan, "
@@ -324,7 +335,7 @@ def run_ours(a, rank, world, local_rank):
         "dtype": "u32", "data": "synthetic (seeded R-MAT generator)",
         "config": dict(work, l2="256 MiB L2 flush written before every timed step; encoded rows "
                                 "%.0f MB > 129 MB L2" % (info["row_total_bytes_used"] / 1e6),
-                       parallelism="replicas" if world > 1 else "single GPU"),
+                       parallelism="replicas" if world > 1 else "single GPU", work_shape=shape),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": btc,
@@ -477,10 +488,13 @@ def run_serve(a):
     kinds = [(eh.QUERY_TRIANGLES, 0), (eh.QUERY_CLIQUES, 4), (eh.QUERY_SIMILAR_NODES, 10)]
     mix = [(rnd.randrange(len(ids)), *kinds[rnd.randrange(3)]) for _ in range(a.queries)]
     # One at a time: each query alone, in order (also the answers for the identity check).
-    alone = []
+    alone, alone_ms = [], {}
     t = time.perf_counter()
     for q in mix:
+        t1 = time.perf_counter()
         alone.append(srv.run_alone(ids[q[0]], q[1], q[2]))
+        key = "%s/s%d" % (("triangles", "cliques4", "similar")[q[1]], specs[q[0]][0])
+        alone_ms.setdefault(key, []).append(1e3 * (time.perf_counter() - t1))
     serial_qps = len(mix) / (time.perf_counter() - t)
     rate = a.rate or 0.8 * serial_qps * a.slots
     # Open-loop Poisson arrivals from a submitter thread.
@@ -506,6 +520,8 @@ def run_serve(a):
     res = [srv.wait(tk, timeout_ms=600000) for tk in tickets]
     wall = time.perf_counter() - t0
     lat = sorted((r["done_ns"] - r["submit_ns"]) / 1e6 for r in res)
+    wait = sorted((r["start_ns"] - r["submit_ns"]) / 1e6 for r in res)
+    run = sorted((r["done_ns"] - r["start_ns"]) / 1e6 for r in res)
     same = all(r["count"] == c for r, c in zip(res, alone))
     st = srv.stats()
     srv.close()
@@ -515,6 +531,9 @@ def run_serve(a):
         "higher_is_better": True, "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
         "arrival_rate_per_s": rate, "queries": len(mix), "slots": a.slots, "one_at_a_time_qps": serial_qps,
         "speedup_vs_one_at_a_time": qps / serial_qps, "results_identical_alone_and_in_mix": same,
+        "queue_wait_p50_ms": wait[len(wait) // 2], "in_slot_p50_ms": run[len(run) // 2],
+        "alone_ms_by_query": {k: [len(v), round(statistics.median(v), 3), round(sum(v), 1)]
+                              for k, v in sorted(alone_ms.items())},
         "max_inflight": st["max_inflight"], "resident_bytes": st["resident_bytes"], "hbm_cap_bytes": st["hbm_cap_bytes"],
         "graphs": len(ids), "graph_load_s": t_load, "query_mix": "uniform: triangles / 4-cliques / similar_nodes(10)",
         "data": "synthetic (seeded R-MAT generator)"}), flush=True)

@@ -105,6 +105,20 @@ eh_status eh_generate_planted_cliques(uint64_t n, uint64_t background_edges, uin
                                       uint32_t min_size, uint32_t max_size, uint64_t seed,
                                       eh_hgraph_t* out);
 
+/* Device ingestion: the work of MutableGraph::undirectedFromEdgeList
+ * (src/MutableGraph.hpp:517-599) and reorder_by_degree (:268-272) on the GPU.
+ * num_edges pairs (d_src[e], d_dst[e]) of vertex ids < n in device memory become
+ * a symmetric CSR with sorted, deduplicated rows; self-loops are kept as the
+ * reference's loader keeps them unless drop_self_loops.  degree_order relabels
+ * by descending degree, ties by ascending id, and d_new2old (from eh_dcsr_view)
+ * then maps new ids to input ids.  The CSR feeds eh_matrix_build_device. */
+typedef struct eh_dcsr* eh_dcsr_t;
+eh_status eh_dcsr_from_edges(uint64_t n, uint64_t num_edges, const uint32_t* d_src, const uint32_t* d_dst,
+                             int drop_self_loops, int degree_order, void* stream, eh_dcsr_t* out);
+eh_status eh_dcsr_view(eh_dcsr_t g, uint64_t* n, uint64_t* num_entries, const uint64_t** d_offsets,
+                       const uint32_t** d_nbrs, const uint32_t** d_new2old);
+void eh_dcsr_free(eh_dcsr_t g);
+
 /* ------------------------------------------------------------------------- */
 /* Device matrix: the reference's SparseMatrix<T,R> (src/SparseMatrix.hpp).  */
 /* ------------------------------------------------------------------------- */
@@ -192,6 +206,15 @@ eh_status eh_count_lollipops_async(eh_matrix_t m, uint64_t* d_count, void* strea
 eh_status eh_similar_nodes(eh_matrix_t m, uint32_t threshold, uint64_t* count, void* stream);
 eh_status eh_similar_nodes_async(eh_matrix_t m, uint32_t threshold, uint64_t* d_count,
                                  void* stream);
+/* Triangle tuples, as undirected_triangle_counting would emit them with tuple
+ * output (Table<T>::write_table, src/Table.hpp:30-43): every (i, j, k) with
+ * i > j > k, j in row(i), k in row(i) ∩ row(j), written as three u32 row ids
+ * to d_out[3t .. 3t+2] for t < capacity, in no particular order; *d_total (device)
+ * receives the number of triangles (tuples past capacity are counted, not
+ * written).  Map rows to external ids with the graph's id map.  Matrix built
+ * with EH_SELECT_LOWER. */
+eh_status eh_list_triangles(eh_matrix_t m, uint32_t* d_out, uint64_t capacity, uint64_t* d_total,
+                            void* stream);
 /* ops::set_intersect on rows (src/set/ops/intersection.hpp, dispatcher :2067-2117):
  * d_counts[p] = |row(d_a[p]) ∩ row(d_b[p])| for p < npairs (device arrays);
  * a pair that names a row >= matrix_size gets 0xffffffff. */
@@ -205,6 +228,7 @@ typedef struct eh_tuning {
   uint32_t light_max;     /* pivots with at most this many entries run one per warp */
   uint32_t unit_span;     /* pivot positions per CTA work unit for larger pivots    */
   uint32_t ctas_per_sm;   /* resident CTAs per SM of the persistent count kernel     */
+  uint32_t core_rows;     /* highest-degree rows kept as a dense bitmap (0 = none)   */
   float ms;               /* median triangle-count time with the chosen shape        */
   uint32_t configs_tried;
 } eh_tuning;

@@ -749,3 +749,40 @@ uint64_t oracle_dump(void* mp, uint8_t* buf) {
   }
   return pos;
 }
+
+/* Triangle tuples as undirected_triangle_counting would emit them with tuple
+ * output on (Table<T>::write_table, src/Table.hpp:30-43): for every pivot i and
+ * j in row(i), each k in row(i) ∩ row(j) gives (i, j, k).  Writes up to cap
+ * tuples (3 u32 each) in pivot order and returns the total. */
+uint64_t oracle_list_triangles(void* mp, uint32_t* out, uint64_t cap) {
+  omatrix* m = (omatrix*)mp;
+  uint64_t total = 0, maxc = 1, maxb = 16;
+  for (uint64_t i = 0; i < m->n; i++) {
+    if (m->row_lengths[i] > maxc) maxc = m->row_lengths[i];
+    if (m->row_offsets[i + 1] - m->row_offsets[i] > maxb) maxb = m->row_offsets[i + 1] - m->row_offsets[i];
+  }
+  uint32_t* as = (uint32_t*)malloc((maxc + 16) * 4);
+  uint32_t* cs = (uint32_t*)malloc((maxc + 16) * 4);
+  uint8_t* cbuf = (uint8_t*)malloc((maxb > maxc * 4 ? maxb : maxc * 4) + 64);
+  for (uint64_t i = 0; i < m->n; i++) {
+    oset A = get_row(m, i);
+    uint64_t na = decode(A, as);
+    for (uint64_t e = 0; e < na; e++) {
+      oset Cs;
+      set_intersect(A, get_row(m, as[e]), cbuf, &Cs);
+      uint64_t nc = decode(Cs, cs);
+      for (uint64_t t = 0; t < nc; t++) {
+        if (total < cap) {
+          out[3 * total] = (uint32_t)i;
+          out[3 * total + 1] = as[e];
+          out[3 * total + 2] = cs[t];
+        }
+        total++;
+      }
+    }
+  }
+  free(as);
+  free(cs);
+  free(cbuf);
+  return total;
+}

@@ -64,6 +64,8 @@ def lib():
         L.oracle_max_threads.restype = C.c_int
         L.oracle_dump.restype = C.c_uint64
         L.oracle_dump.argtypes = [P, P]
+        L.oracle_list_triangles.restype = C.c_uint64
+        L.oracle_list_triangles.argtypes = [P, P, C.c_uint64]
         _lib = L
     return _lib
 
@@ -120,6 +122,13 @@ class Matrix:
 
     def triangles(self):
         return int(lib().oracle_triangles(self.h, self.threads))
+
+    def list_triangles(self):
+        """(T, 3) u32 array of (i, j, k) triangle tuples, i > j > k, pivot order."""
+        total = lib().oracle_list_triangles(self.h, None, 0)
+        out = np.zeros((max(total, 1), 3), np.uint32)
+        lib().oracle_list_triangles(self.h, _ptr(out), total)
+        return out[:total]
 
     def triangles_range(self, lo, hi):
         return int(lib().oracle_triangles_range(self.h, lo, hi, self.threads))

@@ -34,7 +34,7 @@ class EHError(RuntimeError):
 
 class Tuning(C.Structure):
     _fields_ = [("light_max", C.c_uint32), ("unit_span", C.c_uint32), ("ctas_per_sm", C.c_uint32),
-                ("ms", C.c_float), ("configs_tried", C.c_uint32)]
+                ("core_rows", C.c_uint32), ("ms", C.c_float), ("configs_tried", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):
@@ -116,6 +116,7 @@ def load(build_if_missing=True):
         "eh_similar_nodes": (I, [P, U32, C.POINTER(U64), P]),
         "eh_similar_nodes_async": (I, [P, U32, P, P]),
         "eh_intersect_rows": (I, [P, P, P, U64, P, P]),
+        "eh_list_triangles": (I, [P, P, U64, P, P]),
         "eh_matrix_tune": (I, [P, P, C.POINTER(Tuning)]),
         "eh_batch_build": (I, [U32, P, U64, P, P, I, P, C.POINTER(P)]),
         "eh_batch_count": (I, [P, U32, P, P]),
@@ -123,6 +124,9 @@ def load(build_if_missing=True):
         "eh_batch_tune": (I, [P, P, C.POINTER(Tuning)]),
         "eh_batch_matrix": (I, [P, C.POINTER(P)]),
         "eh_batch_free": (None, [P]),
+        "eh_dcsr_from_edges": (I, [U64, U64, P, P, I, I, P, C.POINTER(P)]),
+        "eh_dcsr_view": (I, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+        "eh_dcsr_free": (None, [P]),
         "eh_server_create": (I, [C.POINTER(ServerConfig), C.POINTER(P)]),
         "eh_server_add_graph": (I, [P, U64, P, P, I, C.POINTER(U32)]),
         "eh_server_submit": (I, [P, U32, I, U32, C.POINTER(U64)]),
@@ -352,6 +356,10 @@ class Matrix:
     def similar_nodes_async(self, threshold, d_out, stream=None):
         check(load().eh_similar_nodes_async(self.h, threshold, C.c_void_p(d_out), _stream(stream)))
 
+    def list_triangles(self, d_out, capacity, d_total, stream=None):
+        check(load().eh_list_triangles(self.h, C.c_void_p(d_out), capacity, C.c_void_p(d_total),
+                                       _stream(stream)))
+
     def tune(self, stream=None):
         t = Tuning()
         check(load().eh_matrix_tune(self.h, _stream(stream), C.byref(t)))
@@ -360,6 +368,31 @@ class Matrix:
     def intersect_rows(self, d_a, d_b, npairs, d_counts, stream=None):
         check(load().eh_intersect_rows(self.h, C.c_void_p(d_a), C.c_void_p(d_b), npairs,
                                        C.c_void_p(d_counts), _stream(stream)))
+
+
+class DeviceCSR:
+    """Symmetric CSR built on the device from raw edge arrays (eh_dcsr_*)."""
+
+    def __init__(self, n, d_src, d_dst, num_edges, drop_self_loops=False, degree_order=True, stream=None):
+        self.h = C.c_void_p()
+        check(load().eh_dcsr_from_edges(n, num_edges, C.c_void_p(d_src), C.c_void_p(d_dst), int(drop_self_loops),
+                                        int(degree_order), _stream(stream), C.byref(self.h)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            load().eh_dcsr_free(self.h)
+            self.h = None
+
+    def view(self):
+        """(n, entries, d_offsets, d_nbrs, d_new2old) as device addresses (ints; 0 = none)."""
+        n, m = C.c_uint64(), C.c_uint64()
+        o, b, r = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(load().eh_dcsr_view(self.h, C.byref(n), C.byref(m), C.byref(o), C.byref(b), C.byref(r)))
+        return n.value, m.value, o.value or 0, b.value or 0, r.value or 0
+
+    def matrix(self, selection="lower", layout="hybrid", stream=None):
+        n, _, o, b, _ = self.view()
+        return Matrix.build_device(n, o, b, selection, layout, stream=stream)
 
 
 class Batch:

@@ -18,6 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libeh_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
+CCCL = "/usr/local/cuda/include/cccl"  # CUB (header-only, ships with the CUDA toolkit)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -65,7 +66,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         jobs.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
-                     "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp", "-I", INCLUDE, *extra_nvcc,
+                     "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp", "-I", INCLUDE, "-I", CCCL, *extra_nvcc,
                      "-c", src, "-o", obj])
     for src in cpp:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")

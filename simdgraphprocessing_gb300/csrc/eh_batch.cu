@@ -44,7 +44,7 @@ struct Batch {
 namespace {
 
 struct Shape {
-  uint32_t light_max, unit_span, ctas;
+  uint32_t light_max, unit_span, ctas, core;
 };
 
 std::mutex g_tune_mutex;
@@ -56,7 +56,7 @@ std::string tune_key(const Matrix* m, bool batch) {
   cudaGetDeviceProperties(&prop, m->device);
   int lc = 0, lr = 0;
   while ((1ull << (lc + 1)) <= m->tot.cardinality) lc++;
-  while ((1ull << (lr + 1)) <= m->plan.n_order) lr++;
+  while ((1ull << (lr + 1)) <= m->n) lr++;
   char buf[512];
   snprintf(buf, sizeof(buf), "%.200s|sm%d|layout%d|card2^%d|rows2^%d|%s", prop.name, prop.multiProcessorCount, m->layout,
            lc, lr, batch ? "batch" : "single");
@@ -74,8 +74,8 @@ void load_tune_file() {
   FILE* f = fopen(path, "r");
   if (!f) return;
   char key[512];
-  unsigned lm, us, ct;
-  while (fscanf(f, "%511s %u %u %u", key, &lm, &us, &ct) == 4) g_tune_cache[key] = Shape{lm, us, ct};
+  unsigned lm, us, ct, co;
+  while (fscanf(f, "%511s %u %u %u %u", key, &lm, &us, &ct, &co) == 5) g_tune_cache[key] = Shape{lm, us, ct, co};
   fclose(f);
 }
 
@@ -85,7 +85,7 @@ void store_tune(const std::string& key, const Shape& s) {
   if (!path) return;
   FILE* f = fopen(path, "a");
   if (!f) return;
-  fprintf(f, "%s %u %u %u\n", key.c_str(), s.light_max, s.unit_span, s.ctas);
+  fprintf(f, "%s %u %u %u %u\n", key.c_str(), s.light_max, s.unit_span, s.ctas, s.core);
   fclose(f);
 }
 
@@ -100,6 +100,7 @@ eh_status apply_shape(Matrix* m, const Shape& s, cudaStream_t st) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
   m->light_max = s.light_max;
   m->unit_span = s.unit_span;
+  m->core_limit = s.core;
   m->grid = sms * (int)s.ctas;
   return ensure_plan(m, st);
 }
@@ -130,17 +131,19 @@ eh_status time_shape(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs,
 }
 
 eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaStream_t st, eh_tuning* res) {
-  std::lock_guard<std::mutex> lock(g_tune_mutex);
-  load_tune_file();
+  // The first plan build looks up the shape cache itself (apply_cached_shape), so
+  // it runs before this function takes the cache lock.
   eh_status s = ensure_plan(m, st);
   if (s != EH_OK) return s;
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  load_tune_file();
   const std::string key = tune_key(m, graph_rows != nullptr);
   unsigned long long* out = nullptr;
   const size_t outn = graph_rows ? num_graphs : 1;
   if (cudaMalloc((void**)&out, outn * sizeof(unsigned long long)) != cudaSuccess)
     return set_error(EH_ERR_OUT_OF_MEMORY, "tuner output allocation failed");
   auto it = g_tune_cache.find(key);
-  Shape best{m->light_max, m->unit_span, (uint32_t)max_ctas_per_sm(m->device)};
+  Shape best{m->light_max, m->unit_span, (uint32_t)max_ctas_per_sm(m->device), m->core_limit};
   float best_ms = 0;
   uint32_t tried = 0;
   if (it != g_tune_cache.end()) {
@@ -164,14 +167,20 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
         best = c;
       }
     };
+    const Shape start = best;
+    for (uint32_t co : {0u, 8192u, 16384u})
+      if (co != start.core) consider(Shape{start.light_max, start.unit_span, start.ctas, co});
+    const Shape after_core = best;
     for (int c = 1; c <= cmax; c++)
-      if ((uint32_t)c != best.ctas) consider(Shape{best.light_max, best.unit_span, (uint32_t)c});
+      if ((uint32_t)c != after_core.ctas)
+        consider(Shape{after_core.light_max, after_core.unit_span, (uint32_t)c, after_core.core});
     const Shape after_ctas = best;
     for (uint32_t lm : {32u, 64u, 96u})
-      if (lm != after_ctas.light_max && lm <= kLightMax) consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas});
+      if (lm != after_ctas.light_max && lm <= kLightMax)
+        consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas, after_ctas.core});
     const Shape after_lm = best;
     for (uint32_t us : {32u, 64u, 128u, 256u, 512u})
-      if (us != after_lm.unit_span) consider(Shape{after_lm.light_max, us, after_lm.ctas});
+      if (us != after_lm.unit_span) consider(Shape{after_lm.light_max, us, after_lm.ctas, after_lm.core});
     if (s == EH_OK) {
       s = apply_shape(m, best, st);
       store_tune(key, best);
@@ -183,6 +192,7 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
     res->light_max = best.light_max;
     res->unit_span = best.unit_span;
     res->ctas_per_sm = best.ctas;
+    res->core_rows = best.core;
     res->ms = best_ms;
     res->configs_tried = tried;
   }
@@ -190,6 +200,22 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
 }
 
 }  // namespace
+
+// Applies a cached tuned shape for this matrix's size class, if one exists.
+// Called when a matrix's plan is first built (before the plan's units exist).
+void apply_cached_shape(Matrix* m) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  load_tune_file();
+  auto it = g_tune_cache.find(tune_key(m, m->is_batch));
+  if (it == g_tune_cache.end()) return;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
+  m->light_max = it->second.light_max;
+  m->unit_span = it->second.unit_span;
+  m->core_limit = it->second.core;
+  m->grid = sms * (int)it->second.ctas;
+}
+
 }  // namespace eh
 
 using eh::Batch;
@@ -233,6 +259,7 @@ eh_status eh_batch_build(uint32_t num_graphs, const uint64_t* graph_rows, uint64
   if (s != EH_OK) return s;
   Batch* b = new Batch();
   b->m = reinterpret_cast<eh::Matrix*>(mh);
+  b->m->is_batch = true;
   b->num_graphs = num_graphs;
   std::vector<uint32_t> gr(num_graphs + 1);
   for (uint32_t g = 0; g <= num_graphs; g++) gr[g] = (uint32_t)graph_rows[g];

@@ -165,11 +165,36 @@ eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaSt
   return EH_OK;
 }
 
+// Dense core of the first min(n, core_limit) rows (rounded down to a multiple of
+// 64); small graphs (under 4,096 rows) go without.
+eh_status ensure_core(Matrix* m, cudaStream_t st) {
+  Plan& p = m->plan;
+  uint32_t want = (uint32_t)std::min<uint64_t>(m->n, m->core_limit) & ~63u;
+  if (m->n < 4096) want = 0;
+  if (want == p.core_k && (want == 0 || p.core)) return EH_OK;
+  if (p.core) {
+    CU(cudaStreamSynchronize(st), "core");
+    cudaFree(p.core);
+    m->device_bytes -= core_row_offset(p.core_k) * 8;
+    p.core = nullptr;
+    p.core_k = 0;
+  }
+  if (want == 0) return EH_OK;
+  const uint64_t words = core_row_offset(want);
+  CU(cudaMalloc((void**)&p.core, words * 8), "core allocation");
+  m->device_bytes += words * 8;
+  CU(launch_core_build(m->desc, m->arena, want, p.core, st), "core build");
+  CU(cudaStreamSynchronize(st), "core build");
+  p.core_k = want;
+  return EH_OK;
+}
+
 // Row order (descending card) and decoded copies of the giant non-uint pivots,
 // then the heavy units for the matrix's current work shape.
 eh_status ensure_plan(Matrix* m, cudaStream_t st) {
   Plan& p = m->plan;
   if (!p.ready) {
+    apply_cached_shape(m);
     uint32_t* hist = nullptr;
     uint32_t* cursor = nullptr;
     const uint64_t nn = m->n ? m->n : 1;
@@ -230,6 +255,8 @@ eh_status ensure_plan(Matrix* m, cudaStream_t st) {
     CU(cudaStreamSynchronize(st), "plan build");
     p.ready = true;
   }
+  eh_status s = ensure_core(m, st);
+  if (s != EH_OK) return s;
   return ensure_units(m, m->light_max, m->unit_span, st);
 }
 
@@ -248,6 +275,8 @@ PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
   a.unit_span = m->plan.unit_span;
   a.graph_rows = nullptr;
   a.num_graphs = 0;
+  a.core = m->plan.core;
+  a.core_k = m->plan.core_k;
   return a;
 }
 
@@ -281,7 +310,7 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
   const uint32_t nG = p.above(kCliqueSmemMax);
   const uint32_t nB = p.above(32);
   const uint32_t nL = p.above(k - 2);
-  CliqueArgs a{m->desc, m->arena, p.order, k, out, graph_rows, num_graphs};
+  CliqueArgs a{m->desc, m->arena, p.order, k, out, graph_rows, num_graphs, p.core, p.core_k};
   CU(cudaMemsetAsync(w.counters, 0, 8 * sizeof(uint32_t), st), "memset");
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
@@ -524,6 +553,7 @@ void eh_matrix_free(eh_matrix_t mh) {
   cudaFree(m->plan.units);
   cudaFree(m->plan.giant_lists);
   cudaFree(m->plan.giant_off);
+  cudaFree(m->plan.core);
   cudaFree(m->clique_scratch);
   delete m;
 }

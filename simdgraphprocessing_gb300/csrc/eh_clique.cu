@@ -60,8 +60,15 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
       uint32_t e = 1, t = lane;
       while (t >= e) { t -= e; e++; }
       for (uint32_t q = lane; q < pairs; q += 32) {
-        const RowView B = load_view(a.desc, a.arena, list[e]);
-        if (row_contains(B, list[t])) atomicOr(&mask[e], 1u << t);
+        const uint32_t j = list[e], x = list[t];
+        bool hit;
+        if (j < a.core_k) {
+          hit = (__ldg(a.core + core_row_offset(j) + (x >> 6)) >> (x & 63)) & 1ull;
+        } else {
+          const RowView B = load_view(a.desc, a.arena, j);
+          hit = row_contains(B, x);
+        }
+        if (hit) atomicOr(&mask[e], 1u << t);
         t += 32;
         while (t >= e && e < c) { t -= e; e++; }
       }
@@ -146,9 +153,19 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
     // phase 1: warp per e builds M[e]
     for (uint32_t e = 1 + warp; e < c; e += NW) {
       const uint32_t j = list[e];
+      uint32_t* Me = masks + (uint64_t)e * W;
+      if (j < a.core_k) {  // core row j = row(j) ∩ [0, j): one word per probe, L2-resident
+        const unsigned long long* row = a.core + core_row_offset(j);
+        for (uint32_t b = 0; b < e; b += 32) {
+          const uint32_t t = b + lane;
+          const bool hit = t < e && ((__ldg(row + (list[t] >> 6)) >> (list[t] & 63)) & 1ull);
+          const uint32_t word = __ballot_sync(FULL, hit);
+          if (lane == 0) Me[b >> 5] = word;
+        }
+        continue;
+      }
       const RowView B = load_view(a.desc, a.arena, j);
       if (B.card == 0) continue;
-      uint32_t* Me = masks + (uint64_t)e * W;
       bool stream = false;
       if (B.type == TY_UINT) stream = (uint64_t)B.card * ilog2p1_c(e) < (uint64_t)e * ilog2p1_c(B.card) * 4u;
       else if (B.type == TY_PSHORT) stream = (uint64_t)B.card * ilog2p1_c(e) < (uint64_t)e * (B.aux + ilog2p1_c(B.card)) * 4u;
@@ -174,12 +191,29 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
       if (top == 0) {
         for (uint32_t w = lane; w < we; w += 32) acc += __popc(Me[w]);
       } else if (top == 1) {
-        for (uint32_t w = 0; w < we; w++) {
-          const uint32_t bits = Me[w];
-          if (!((bits >> lane) & 1u)) continue;
-          const uint32_t t = 32 * w + lane;
-          const uint32_t* Mt = masks + (uint64_t)t * W;
-          for (uint32_t x = 0; x <= (t >> 5); x++) acc += __popc(Me[x] & Mt[x]);
+        // k = 4: sum over t in M[e] of popc(M[e] & M[t]); M[t] has no bits at or above t.
+        if (GLOBAL && we > 8) {
+          // Long rows in global memory: the warp walks the set bits t together and
+          // lanes take consecutive words of the two rows (coalesced reads).
+          for (uint32_t w0 = 0; w0 < we; w0++) {
+            uint32_t bits = Me[w0];
+            while (bits) {
+              const uint32_t t = 32 * w0 + (__ffs(bits) - 1);
+              bits &= bits - 1;
+              const uint32_t* Mt = masks + (uint64_t)t * W;
+              for (uint32_t x = lane; x <= (t >> 5); x += 32) acc += __popc(Me[x] & Mt[x]);
+            }
+          }
+        } else {
+          // Each lane takes one t of a word of M[e]; the odd row stride W keeps the
+          // lanes' rows in different shared-memory banks.
+          for (uint32_t w = 0; w < we; w++) {
+            const uint32_t bits = Me[w];
+            if (!((bits >> lane) & 1u)) continue;
+            const uint32_t t = 32 * w + lane;
+            const uint32_t* Mt = masks + (uint64_t)t * W;
+            for (uint32_t x = 0; x <= (t >> 5); x++) acc += __popc(Me[x] & Mt[x]);
+          }
         }
       } else {
         // Warp-cooperative depth-first search; S[d], R[d] live in the warp's stack.
@@ -243,8 +277,12 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
 
 }  // namespace
 
+// Mask row stride in words: enough for cmax bits, odd so that lanes reading
+// different rows hit different shared-memory banks.
+static uint32_t mask_stride(uint32_t cmax) { return ((cmax + 31) / 32) | 1u; }
+
 uint64_t clique_slot_words(uint32_t cmax, uint32_t k) {
-  const uint64_t W = (cmax + 31) / 32;
+  const uint64_t W = mask_stride(cmax);
   return (uint64_t)cmax + (uint64_t)cmax * W + (uint64_t)NW * 2 * (k - 2) * W;
 }
 
@@ -258,7 +296,7 @@ cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_
 cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                               uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st) {
   if (pos_end <= pos_begin) return cudaSuccess;
-  const uint32_t W = (cmax + 31) / 32;
+  const uint32_t W = mask_stride(cmax);
   const uint64_t slot = clique_slot_words(cmax, a.k);
   if (gscratch) {
     k_clique_cta<true><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch, slot);

@@ -24,6 +24,7 @@
 //    pair per lane, so short rows keep every lane busy.
 // Per-lane counts stay in registers; one u64 atomic per CTA at the end replaces
 // the reference's per-thread padded t_count array.
+#include <algorithm>
 #include <cstdint>
 
 #include "eh_kernels.cuh"
@@ -37,6 +38,7 @@ constexpr uint32_t kLightChunk = 16;  // light pivots per atomic grab
 
 struct __align__(16) PivotSmem {
   unsigned long long words[kCtaWordCap];
+  unsigned long long abits[kCoreMaxK / 64];  // pivot ∩ [0, core_k) as bits
   uint32_t list[kCtaListCap];
   uint32_t wlist[NWARPS][kLightMax];
   uint32_t scan[kCtaThreads];
@@ -89,7 +91,9 @@ __device__ uint32_t pair_count_warp(const uint32_t* L, uint32_t e, const RowView
 }
 
 template <bool LOLLI>
-__global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2* __restrict__ units,
+// 8 resident CTAs per SM (64 warps, 32 registers per thread): the kernel is
+// bound by the latency of scattered probes, so occupancy pays.
+__global__ void __launch_bounds__(kCtaThreads, 8) k_pivots(PivotArgs a, const uint2* __restrict__ units,
                                                         uint32_t n_units) {
   __shared__ PivotSmem s;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -116,6 +120,17 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
       for (uint32_t k = threadIdx.x; k < A.len; k += kCtaThreads) s.words[k] = w[k];
       A.p = s.words;
     }
+    // The core path is skipped for pshort pivots of >= 65,536 entries, where the
+    // reference's u16 partition count can drop a block (see pshort_pair_drop).
+    const bool use_core = a.core_k && !(A.type == TY_PSHORT && A.card >= 65536u);
+    if (use_core) {
+      for (uint32_t k = threadIdx.x; k < (a.core_k >> 6); k += kCtaThreads) s.abits[k] = 0ull;
+      __syncthreads();
+      for (uint32_t k = threadIdx.x; k < A.card; k += kCtaThreads) {
+        const uint32_t x = L[k];
+        if (x < a.core_k) atomicOr(&s.abits[x >> 6], 1ull << (x & 63));
+      }
+    }
     __syncthreads();
     const uint32_t c = A.card;
     const uint32_t e0 = 1 + uu.y * a.unit_span;
@@ -123,8 +138,26 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
     unsigned long long uacc = 0;
     for (uint32_t e = e0 + warp; e < e1; e += NWARPS) {
       const uint32_t j = L[e];
-      const RowView B = load_view(a.desc, a.arena, j);
-      const uint32_t cnt = pair_count_warp(L, e, A, B, j, lane);
+      uint32_t cnt;
+      if (use_core && j < a.core_k) {
+        // Core row j holds row(j) ∩ [0, j): AND it with the pivot's bits, or probe
+        // the e pivot elements below j, whichever touches fewer words.
+        const unsigned long long* row = a.core + core_row_offset(j);
+        const uint32_t wj = (j + 63) >> 6;
+        cnt = 0;
+        if (wj <= 2 * e) {
+          for (uint32_t w = lane; w < wj; w += 32) cnt += __popcll(s.abits[w] & __ldg(row + w));
+        } else {
+          for (uint32_t t = lane; t < e; t += 32) {
+            const uint32_t x = L[t];
+            cnt += (uint32_t)((__ldg(row + (x >> 6)) >> (x & 63)) & 1ull);
+          }
+        }
+        cnt = warp_sum_u32(cnt);
+      } else {
+        const RowView B = load_view(a.desc, a.arena, j);
+        cnt = pair_count_warp(L, e, A, B, j, lane);
+      }
       if (lane == 0) uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
     }
     if (a.graph_rows) {  // batch: this unit's count goes to its graph
@@ -155,8 +188,13 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
       while (t >= e) { t -= e; e++; }
       uint32_t cnt = 0;
       for (uint32_t q = lane; q < pairs; q += 32) {
-        const RowView B = load_view(a.desc, a.arena, list[e]);
-        cnt += row_contains(B, list[t]);
+        const uint32_t j = list[e], x = list[t];
+        if (j < a.core_k) {  // x < j: one word of the L2-resident core
+          cnt += (uint32_t)((__ldg(a.core + core_row_offset(j) + (x >> 6)) >> (x & 63)) & 1ull);
+        } else {
+          const RowView B = load_view(a.desc, a.arena, j);
+          cnt += row_contains(B, x);
+        }
         t += 32;
         while (t >= e && e < c) { t -= e; e++; }
       }
@@ -180,6 +218,33 @@ __global__ void __launch_bounds__(kCtaThreads) k_pivots(PivotArgs a, const uint2
     unsigned long long tot = 0;
     for (int w = 0; w < NWARPS; w++) tot += s_red[w];
     if (tot && !a.graph_rows) atomicAdd(a.out, tot);
+  }
+}
+
+// Dense core build: one warp per row j < core_k writes row(j) ∩ [0, j) as bits.
+__global__ void __launch_bounds__(256) k_core_build(const RowDesc* __restrict__ desc, const uint4* __restrict__ arena,
+                                                    uint32_t core_k, unsigned long long* __restrict__ core) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nw = gridDim.x * (blockDim.x / 32);
+  for (uint32_t j = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); j < core_k; j += nw) {
+    unsigned long long* row = core + core_row_offset(j);
+    const uint32_t wj = (j + 63) >> 6;
+    for (uint32_t w = lane; w < wj; w += 32) row[w] = 0ull;
+    __syncwarp();
+    const RowView B = load_view(desc, arena, j);
+    if (B.type == TY_BITSET) {
+      const unsigned long long* bw = static_cast<const unsigned long long*>(B.p);
+      for (uint32_t w = lane; w < B.len; w += 32) {
+        const uint32_t gw = B.aux + w;
+        if (gw >= wj) break;
+        unsigned long long x = bw[w];
+        if (gw == wj - 1 && (j & 63)) x &= (1ull << (j & 63)) - 1ull;
+        row[gw] = x;
+      }
+    } else {
+      warp_for_each(B, j, lane, [&](uint32_t x) { atomicOr(&row[x >> 6], 1ull << (x & 63)); });
+    }
+    __syncwarp();
   }
 }
 
@@ -287,6 +352,14 @@ cudaError_t launch_triangles(const PivotArgs& a, const uint2* units, uint32_t n_
 cudaError_t launch_lollipops(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
                              cudaStream_t st) {
   return launch_pivots<true>(a, units, n_units, grid, st);
+}
+
+cudaError_t launch_core_build(const RowDesc* desc, const uint4* arena, uint32_t core_k, unsigned long long* core,
+                              cudaStream_t st) {
+  if (core_k == 0) return cudaSuccess;
+  const uint32_t blocks = std::min<uint32_t>((core_k + 7) / 8, 152u * 16u);
+  k_core_build<<<blocks, 256, 0, st>>>(desc, arena, core_k, core);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_similar(uint64_t n, const RowDesc* desc, const uint4* arena, uint32_t vstar,

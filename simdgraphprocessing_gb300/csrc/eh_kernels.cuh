@@ -72,13 +72,15 @@ struct PivotArgs {
   uint32_t unit_span;      // pivot positions e per heavy unit
   const uint32_t* graph_rows;  // batch mode: graph g owns rows [graph_rows[g], graph_rows[g+1]); else null
   uint32_t num_graphs;
+  const unsigned long long* core;  // dense core bitmap of rows j < core_k (see core_row_offset), or null
+  uint32_t core_k;
 };
 constexpr uint32_t kCtaThreads = 256;
 constexpr uint32_t kLightMax = 96;     // largest light_max: warp-wide pivots fit a slice of this size
 constexpr uint32_t kDefaultLightMax = 96;
 constexpr uint32_t kDefaultUnitSpan = 128;
-constexpr uint32_t kCtaListCap = 6144; // CTA-staged list capacity (elements)
-constexpr uint32_t kCtaWordCap = 2048; // CTA-staged bitset words capacity
+constexpr uint32_t kCtaListCap = 2048; // CTA-staged list capacity (elements)
+constexpr uint32_t kCtaWordCap = 1024; // CTA-staged bitset words capacity
 cudaError_t launch_pivot_units(const RowDesc* desc, const uint32_t* order, uint32_t n_heavy,
                                uint32_t unit_span, uint32_t* cnt, cudaStream_t st);
 cudaError_t launch_pivot_unit_fill(const uint32_t* cnt, const uint32_t* start, uint32_t n_heavy,
@@ -88,6 +90,18 @@ cudaError_t launch_triangles(const PivotArgs& a, const uint2* units, uint32_t n_
 cudaError_t launch_lollipops(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
                              cudaStream_t st);
 int pivot_grid(int device);  // persistent grid: SMs x resident CTAs of the pivot kernel
+
+// Dense core: for every row j < core_k, the bits of row(j) ∩ [0, j) packed in
+// ceil(j/64) words starting at word core_row_offset(j) (a lower-triangular
+// bitmap of the highest-degree rows, which degree ordering puts first).
+constexpr uint32_t kCoreMaxK = 24576;  // 37.7 MB of bits
+__host__ __device__ inline uint64_t core_row_offset(uint32_t j) {
+  if (j == 0) return 0;
+  const uint64_t a = (uint64_t)(j - 1) >> 6, b = (uint64_t)(j - 1) & 63;
+  return 32 * a * (a + 1) + b * (a + 1);  // sum over x < j of ceil(x / 64)
+}
+cudaError_t launch_core_build(const RowDesc* desc, const uint4* arena, uint32_t core_k, unsigned long long* core,
+                              cudaStream_t st);
 cudaError_t launch_similar(uint64_t n, const RowDesc* desc, const uint4* arena, uint32_t vstar,
                            uint32_t threshold, unsigned long long* out, cudaStream_t st);
 cudaError_t launch_intersect_rows(uint64_t n, const RowDesc* desc, const uint4* arena, const uint32_t* a,
@@ -103,6 +117,8 @@ struct CliqueArgs {
   unsigned long long* out; // result; in batch mode out[num_graphs]
   const uint32_t* graph_rows;  // batch mode: graph g owns rows [graph_rows[g], graph_rows[g+1]); else null
   uint32_t num_graphs;
+  const unsigned long long* core;  // dense core bitmap (rows j < core_k), or null
+  uint32_t core_k;
 };
 constexpr uint32_t kCliqueMaxK = 16;
 constexpr uint32_t kCliqueSmemMax = 1024;  // pivots up to this size keep their masks in shared memory

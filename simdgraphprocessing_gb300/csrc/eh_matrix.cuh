@@ -24,6 +24,8 @@ struct Plan {
   uint2* units = nullptr;         // (order position, part)
   uint32_t n_units = 0;
   uint64_t units_cap = 0;
+  unsigned long long* core = nullptr;  // dense core bitmap (rows j < core_k)
+  uint32_t core_k = 0;
   // rows in the plan with card > x (x < 65535)
   uint32_t above(uint32_t x) const { return starts.empty() ? 0 : starts[65535 - x]; }
   // largest card <= x present in the plan (0 if none)
@@ -63,6 +65,8 @@ struct Matrix {
   // Work-shape parameters of the pivot kernel (set by the autotuner).
   uint32_t light_max = kDefaultLightMax;
   uint32_t unit_span = kDefaultUnitSpan;
+  uint32_t core_limit = kCoreMaxK;  // rows in the dense core at most (0 = no core)
+  bool is_batch = false;            // the union matrix of an eh_batch_t
 };
 
 // eh_capi.cu
@@ -70,6 +74,9 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
                        int layout, cudaStream_t st, Matrix** out);
 eh_status ensure_plan(Matrix* m, cudaStream_t st);
 eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaStream_t st);
+eh_status ensure_core(Matrix* m, cudaStream_t st);
+// eh_batch.cu: tuned work shape of this matrix's size class, if the tuner has one.
+void apply_cached_shape(Matrix* m);
 PivotArgs pivot_args(Matrix* m, unsigned long long* out);
 // Count launches; graph_rows / num_graphs != null selects per-graph outputs
 // out[num_graphs].  ws == null uses the matrix's own workspace.  The plan must

@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 def small_batch(eh):
     from simdgraphprocessing_gb300 import workloads as W
-    specs = W.batch_specs(num_graphs=48, seed=40, n_lo=30, n_hi=3000)
+    specs = W.batch_specs(num_graphs=48, seed=40, n_lo=40, n_hi=3000)  # BA needs n > m + 1 (m <= 32)
     csrs = [eh.graph(kind, s, **kw).csr()[:2] for kind, s, kw in specs]
     csrs.append((np.zeros(1, np.uint64), np.zeros(0, np.uint32)))  # an empty graph
     csrs.append((np.array([0, 1, 2], np.uint64), np.array([1, 0], np.uint32)))  # one edge
@@ -61,6 +61,17 @@ def test_batch_graph_replay_and_tuning(eh, oracle, layout):
     assert torch.equal(tri, ref_t) and torch.equal(clq, ref_c)
     want = [oracle.Matrix(o, n, oracle.SELECT_LOWER, oracle.LAYOUTS[layout]).triangles() for o, n in csrs]
     assert ref_t.cpu().tolist() == want
+
+
+@pytest.mark.timeout(300)
+def test_tuning_a_fresh_matrix(eh):
+    # Tuning before any count builds the plan inside the tuner.
+    off, nbr = eh.graph("rmat", 13, scale=13, edges=80000).csr()[:2]
+    m = eh.Matrix.build(off, nbr, "lower", "hybrid")
+    shape = m.tune()
+    assert shape["configs_tried"] >= 1
+    fresh = eh.Matrix.build(off, nbr, "lower", "hybrid")  # picks the cached shape up at plan time
+    assert fresh.count_triangles() == m.count_triangles()
 
 
 def test_single_matrix_tuning_keeps_counts(eh, oracle):
