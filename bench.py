@@ -49,10 +49,11 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile", action="store_true", help="minimal run for ncu captures")
-    p.add_argument("--workload", default="triangles", choices=["triangles", "cliques", "batch", "serve"],
+    p.add_argument("--workload", default="triangles", choices=["triangles", "cliques", "batch", "serve", "paths"],
                    help="triangles: the headline; cliques: 4-clique + lollipop on R-MAT s20 and the "
                         "planted-clique graph; batch: 4,096 graphs in one launch vs one launch per graph; "
-                        "serve: Poisson query stream against 32 resident graphs")
+                        "serve: Poisson query stream against 32 resident graphs; paths: symbiosity and "
+                        "n_path BFS on a directed R-MAT graph")
     p.add_argument("--graphs", type=int, default=0, help="batch / serve: number of graphs (0 = configured)")
     p.add_argument("--queries", type=int, default=400, help="serve: queries in the stream")
     p.add_argument("--rate", type=float, default=0.0, help="serve: arrivals per second (0 = 0.8 x measured capacity)")
@@ -415,6 +416,56 @@ def run_cliques(a):
           flush=True)
 
 
+def run_paths(a):
+    """symbiosity and the n_path BFS on a directed R-MAT graph: scale 22, the
+    first 64M distinct ordered pairs (edge factor 16), seed 5; BFS from the
+    largest row with no depth limit."""
+    import torch
+    import simdgraphprocessing_gb300 as eh
+    from oracle import oracle as O
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(1, dtype=torch.int64, device="cuda")
+    t = time.perf_counter()
+    g = eh.HostGraph.directed_rmat(a.scale, a.edge_factor << a.scale, 5)
+    off, nbr, _, _ = g.csr()
+    ioff, inbr = g.in_csr()
+    t_gen = time.perf_counter() - t
+    rows = eh.Matrix.build(off, nbr, "all", a.layout, stream=stream)
+    cols = eh.Matrix.build(ioff, inbr, "all", a.layout, stream=stream)
+    res = {"graph": "directed_rmat_s%d_ef%d_seed5" % (a.scale, a.edge_factor), "vertices": len(off) - 1,
+           "out_entries": int(len(nbr)), "layout": a.layout, "generate_s": t_gen}
+    sym = rows.symbiosity(cols, 0.5, stream=stream)
+    ts = _events_ms(lambda: rows.symbiosity_async(cols, 0.5, out.data_ptr(), stream.cuda_stream), stream,
+                    a.steps + a.warmup, flush)
+    res.update({"symbiosity": sym, "symbiosity_ms": statistics.median(ts[a.warmup:])})
+    start = rows.max_row_id()
+    path, reached = rows.bfs(start, stream=stream)
+    tb = []
+    for r in range(a.steps + a.warmup):
+        flush.fill_(r & 0xff)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        rows.bfs(start, stream=stream)
+        tb.append((time.perf_counter() - t) * 1e3)
+    res.update({"bfs_start": start, "n_path": path, "bfs_reached": reached,
+                "bfs_ms": statistics.median(tb[a.warmup:]), "bfs_timing": "host wall clock per call (the call "
+                "synchronises once per 8 levels), L2 flushed before each"})
+    if not a.no_cpu:
+        orows = O.Matrix(off, nbr, O.SELECT_ALL, O.LAYOUTS[a.layout])
+        ocols = O.Matrix(ioff, inbr, O.SELECT_ALL, O.LAYOUTS[a.layout])
+        t = time.perf_counter()
+        res["symbiosity_matches_cpu"] = orows.symbiosity(ocols) == sym
+        res["cpu_symbiosity_s"] = time.perf_counter() - t
+        t = time.perf_counter()
+        res["bfs_matches_cpu"] = orows.n_path(start) == (path, reached)
+        res["cpu_bfs_s"] = time.perf_counter() - t
+        res["cpu_threads"] = {"symbiosity": O.lib().oracle_max_threads(), "bfs": 1}
+    print(json.dumps({"workload": "paths", "metric": "symbiosity / n_path BFS time", "unit": "ms",
+                      "higher_is_better": False, "data": "synthetic (seeded directed R-MAT generator)",
+                      "results": [res]}), flush=True)
+
+
 def run_batch(a):
     """4,096 graphs (half G(n, M), half Barabasi-Albert; n log-uniform in
     [200, 50000]; mean degree uniform in [4, 64]; seeds 4+k): triangles and
@@ -544,7 +595,7 @@ def main():
     if a.workload != "triangles":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        {"cliques": run_cliques, "batch": run_batch, "serve": run_serve}[a.workload](a)
+        {"cliques": run_cliques, "batch": run_batch, "serve": run_serve, "paths": run_paths}[a.workload](a)
         return
     if a.profile:
         a.warmup, a.steps, a.no_e2e, a.no_cpu = 1, 1, True, True

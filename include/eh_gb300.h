@@ -88,6 +88,27 @@ eh_status eh_hgraph_view(eh_hgraph_t g, uint64_t* n, uint64_t* num_edges,
                          const uint64_t** ext_ids, uint64_t* max_nbrhood_size);
 void eh_hgraph_free(eh_hgraph_t g);
 
+/* Directed host graphs (MutableGraph with symmetric == false): the CSR above
+ * holds the out-neighbourhoods, a second CSR the in-neighbourhoods.
+ * MutableGraph::directedFromBinary (src/MutableGraph.hpp:656-714): per node
+ * u64 ext id, size_t out_len, u32 out[out_len], size_t in_len, u32 in[in_len]. */
+eh_status eh_hgraph_read_directed_binary(const char* path, eh_hgraph_t* out);
+/* MutableGraph::writeDirectedToBinary (src/MutableGraph.hpp:634-654).  An
+ * undirected graph is written with in = out. */
+eh_status eh_hgraph_write_directed_binary(eh_hgraph_t g, const char* path);
+/* MutableGraph::directedFromEdgeList (src/MutableGraph.hpp:893-986): text
+ * "src dst" pairs, ids interned in order of first appearance, out and in rows
+ * sorted and deduplicated, self-loops kept. */
+eh_status eh_hgraph_read_directed_edge_list(const char* path, eh_hgraph_t* out);
+/* A directed graph from its out-CSR (rows sorted ascending, no duplicates);
+ * the in-CSR is built as its transpose.  ext_ids may be NULL (identity). */
+eh_status eh_hgraph_directed_from_csr(uint64_t n, const uint64_t* out_offsets, const uint32_t* out_nbrs,
+                                      const uint64_t* ext_ids, eh_hgraph_t* out);
+/* In-neighbourhood CSR (the reference's SparseMatrix::get_column source).
+ * *directed = 0 for an undirected graph, whose in-CSR is its CSR. */
+eh_status eh_hgraph_in_view(eh_hgraph_t g, int* directed, uint64_t* num_edges,
+                            const uint64_t** in_offsets, const uint32_t** in_nbrs);
+
 /* Seeded generators (no reference counterpart; the reference has none).
  * All draw from a counter-based SplitMix64 stream so that the same call gives
  * the same graph on any host.  Output: symmetric, deduplicated, self-loops
@@ -104,6 +125,10 @@ eh_status eh_generate_ba(uint64_t n, uint32_t m, uint64_t seed, eh_hgraph_t* out
 eh_status eh_generate_planted_cliques(uint64_t n, uint64_t background_edges, uint32_t num_cliques,
                                       uint32_t min_size, uint32_t max_size, uint64_t seed,
                                       eh_hgraph_t* out);
+/* Directed R-MAT: the first `num_edges` distinct ordered pairs (u, v), u != v,
+ * in draw order, as a directed graph (out- and in-CSR). */
+eh_status eh_generate_directed_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c,
+                                    uint64_t seed, eh_hgraph_t* out);
 
 /* Device ingestion: the work of MutableGraph::undirectedFromEdgeList
  * (src/MutableGraph.hpp:517-599) and reorder_by_degree (:268-272) on the GPU.
@@ -220,6 +245,25 @@ eh_status eh_list_triangles(eh_matrix_t m, uint32_t* d_out, uint64_t capacity, u
  * a pair that names a row >= matrix_size gets 0xffffffff. */
 eh_status eh_intersect_rows(eh_matrix_t m, const uint32_t* d_a, const uint32_t* d_b,
                             uint64_t npairs, uint32_t* d_counts, void* stream);
+/* symbiosity<T,R>::run (apps/symbiosity.cpp:39-58): rows i with
+ * |out(i) ∩ in(i)| / (|out(i)| + |in(i)| - |out(i) ∩ in(i)|) > threshold, the
+ * ratio in double precision (0/0 counts as not above).  `rows` holds the
+ * out-neighbourhoods (SparseMatrix::get_row), `cols` the in-neighbourhoods
+ * (get_column; pass `rows` again for an undirected graph).  Both EH_SELECT_ALL,
+ * same matrix_size and device; the reference's threshold is 0.5. */
+eh_status eh_symbiosity(eh_matrix_t rows, eh_matrix_t cols, double threshold, uint64_t* count,
+                        void* stream);
+eh_status eh_symbiosity_async(eh_matrix_t rows, eh_matrix_t cols, double threshold,
+                              uint64_t* d_count, void* stream);
+/* n_path<T,R>::run (apps/n_path.cpp:30-88): breadth-first search along rows
+ * from `start`; each level ORs the rows of the frontier into the visited
+ * bitset (ops::set_union, src/set/ops/union.hpp) and the next frontier is the
+ * newly set bits (ops::set_difference, src/set/ops/difference.hpp:5-84).
+ * *path_length = the number of levels that found new vertices, stopping once
+ * it reaches max_depth (the reference's --n; 0xeffffff when not given).
+ * *reached (may be NULL) = vertices visited, start included.  EH_SELECT_ALL. */
+eh_status eh_bfs_path_length(eh_matrix_t m, uint32_t start, uint64_t max_depth, uint64_t* path_length,
+                             uint64_t* reached, void* stream);
 
 /* ------------------------------------------------------------------------- */
 /* Work-shape autotuning (no reference counterpart).                           */

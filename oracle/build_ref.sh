@@ -27,7 +27,7 @@ if [ -f "$stamp" ] && [ "$stamp" -nt "$HERE/build_ref.sh" ] && [ "$stamp" -nt "$
   exit 0
 fi
 pids=""
-for app in undirected_triangle_counting n_clique undirected_lollipop_counting similar_nodes; do
+for app in undirected_triangle_counting n_clique undirected_lollipop_counting similar_nodes symbiosity n_path; do
   $CXX $FLAGS "$REF/apps/$app.cpp" -o "$OUT/$app" &
   pids="$pids $!"
 done

@@ -695,6 +695,68 @@ uint64_t oracle_similar_nodes(void* mp, uint32_t threshold, int nthreads) {
   return total;
 }
 
+/* symbiosity<T,R>::run (apps/symbiosity.cpp:39-58): rows i whose out-row
+ * (get_row, matrix `rp`) and in-row (get_column, matrix `cp`; the same matrix
+ * for an undirected graph) have Jaccard ratio above `threshold`; the ratio is
+ * a double division of the intersection size by |A| + |B| - |A ∩ B|. */
+uint64_t oracle_symbiosity(void* rp, void* cp, double threshold, int nthreads) {
+  omatrix* r = (omatrix*)rp;
+  omatrix* c = (omatrix*)cp;
+  uint64_t total = 0;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 100) reduction(+ : total)
+  for (int64_t i = 0; i < (int64_t)r->n; i++) {
+    oset A = get_row(r, i), B = get_row(c, i);
+    uint64_t both = set_intersect(A, B, 0, 0);
+    double ratio = (double)both / (double)(A.card + B.card - both);
+    if (ratio > threshold) total++;
+  }
+  return total;
+}
+
+/* n_path<T,R>::run (apps/n_path.cpp:30-88).  visited / old_visited are bitsets
+ * over every row; each level ORs the frontier's rows into visited
+ * (ops::set_union(bitset, T), src/set/ops/union.hpp:6-127: every element of
+ * the row sets its bit), and the next frontier is visited AND NOT old_visited
+ * in ascending order (ops::set_difference, src/set/ops/difference.hpp:5-84).
+ * The loop stops when that frontier is empty or path_length has reached
+ * `depth`; otherwise path_length grows by one.  *reached = set bits. */
+uint64_t oracle_n_path(void* mp, uint32_t start, uint64_t depth, uint64_t* reached) {
+  omatrix* m = (omatrix*)mp;
+  const uint64_t words = (m->n + 64) / 64;
+  uint64_t* vis = (uint64_t*)calloc(words, 8);
+  uint64_t* old = (uint64_t*)calloc(words, 8);
+  uint32_t* frontier = (uint32_t*)malloc((m->n + 1) * 4);
+  uint32_t* row = (uint32_t*)malloc((m->n + 1) * 4);
+  uint64_t nf = 1, path = 0;
+  frontier[0] = start;
+  vis[start >> 6] |= 1ull << (start & 63);
+  for (;;) {
+    memcpy(old, vis, words * 8);
+    for (uint64_t f = 0; f < nf; f++) {
+      uint64_t k = decode(get_row(m, frontier[f]), row);
+      for (uint64_t e = 0; e < k; e++) vis[row[e] >> 6] |= 1ull << (row[e] & 63);
+    }
+    nf = 0;
+    for (uint64_t w = 0; w < words; w++) {
+      uint64_t x = vis[w] & ~old[w];
+      while (x) {
+        frontier[nf++] = (uint32_t)(64 * w + __builtin_ctzll(x));
+        x &= x - 1;
+      }
+    }
+    if (nf == 0 || path >= depth) break;
+    path++;
+  }
+  if (reached) {
+    uint64_t t = 0;
+    for (uint64_t w = 0; w < words; w++) t += popc64(vis[w]);
+    *reached = t;
+  }
+  free(vis); free(old); free(frontier); free(row);
+  return path;
+}
+
 /* ops::set_intersect on pairs of rows. */
 void oracle_intersect_rows(void* mp, const uint32_t* a, const uint32_t* b, uint64_t np,
                            uint32_t* counts, int nthreads) {

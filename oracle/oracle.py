@@ -64,6 +64,10 @@ def lib():
         L.oracle_max_threads.restype = C.c_int
         L.oracle_dump.restype = C.c_uint64
         L.oracle_dump.argtypes = [P, P]
+        L.oracle_symbiosity.restype = C.c_uint64
+        L.oracle_symbiosity.argtypes = [P, P, C.c_double, C.c_int]
+        L.oracle_n_path.restype = C.c_uint64
+        L.oracle_n_path.argtypes = [P, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint64)]
         L.oracle_list_triangles.restype = C.c_uint64
         L.oracle_list_triangles.argtypes = [P, P, C.c_uint64]
         _lib = L
@@ -142,6 +146,18 @@ class Matrix:
     def similar_nodes(self, threshold=10):
         return int(lib().oracle_similar_nodes(self.h, threshold, self.threads))
 
+    def symbiosity(self, cols=None, threshold=0.5):
+        """symbiosity over this matrix's rows and `cols`' rows (the columns;
+        None = this matrix, as for an undirected graph)."""
+        c = self if cols is None else cols
+        return int(lib().oracle_symbiosity(self.h, c.h, float(threshold), self.threads))
+
+    def n_path(self, start, depth=0xEFFFFFF):
+        """(path_length, reached) of the n_path BFS from row `start`."""
+        r = C.c_uint64(0)
+        n = int(lib().oracle_n_path(self.h, int(start), int(depth), C.byref(r)))
+        return n, int(r.value)
+
     def intersect_rows(self, a, b):
         a = np.ascontiguousarray(a, np.uint32)
         b = np.ascontiguousarray(b, np.uint32)
@@ -169,6 +185,34 @@ def read_binary(path):
         offsets[i + 1] = offsets[i] + ln
     nbrs = np.concatenate(chunks) if chunks else np.zeros(0, np.uint32)
     return offsets, nbrs, ext
+
+
+def read_directed_binary(path):
+    """MutableGraph::directedFromBinary (src/MutableGraph.hpp:656-714) in numpy:
+    u64 n, then per row u64 external id, u64 out length, u32[out length],
+    u64 in length, u32[in length].  Returns (out_off, out_nbr, in_off, in_nbr, ext)."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    n = int(raw[:8].view(np.uint64)[0])
+    pos = 8
+    oo = np.zeros(n + 1, np.uint64)
+    io = np.zeros(n + 1, np.uint64)
+    ext = np.zeros(n, np.uint64)
+    outs, ins = [], []
+    for i in range(n):
+        e, ln = raw[pos:pos + 16].view(np.uint64)
+        pos += 16
+        ext[i] = e
+        ln = int(ln)
+        outs.append(raw[pos:pos + 4 * ln].view(np.uint32))
+        pos += 4 * ln
+        oo[i + 1] = oo[i] + ln
+        ln = int(raw[pos:pos + 8].view(np.uint64)[0])
+        pos += 8
+        ins.append(raw[pos:pos + 4 * ln].view(np.uint32))
+        pos += 4 * ln
+        io[i + 1] = io[i] + ln
+    cat = lambda c: np.concatenate(c) if c else np.zeros(0, np.uint32)
+    return oo, cat(outs), io, cat(ins), ext
 
 
 def counts(offsets, nbrs, layout="hybrid", threads=0, k=4, threshold=10):

@@ -94,6 +94,13 @@ def load(build_if_missing=True):
         "eh_hgraph_view": (I, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(C.POINTER(U64)),
                                C.POINTER(C.POINTER(U32)), C.POINTER(C.POINTER(U64)), C.POINTER(U64)]),
         "eh_hgraph_free": (None, [P]),
+        "eh_hgraph_read_directed_binary": (I, [C.c_char_p, C.POINTER(P)]),
+        "eh_hgraph_write_directed_binary": (I, [P, C.c_char_p]),
+        "eh_hgraph_read_directed_edge_list": (I, [C.c_char_p, C.POINTER(P)]),
+        "eh_hgraph_directed_from_csr": (I, [U64, P, P, P, C.POINTER(P)]),
+        "eh_hgraph_in_view": (I, [P, C.POINTER(I), C.POINTER(U64), C.POINTER(C.POINTER(U64)),
+                                  C.POINTER(C.POINTER(U32))]),
+        "eh_generate_directed_rmat": (I, [U32, U64, C.c_double, C.c_double, C.c_double, U64, C.POINTER(P)]),
         "eh_generate_rmat": (I, [U32, U64, C.c_double, C.c_double, C.c_double, U64, C.POINTER(P)]),
         "eh_generate_er": (I, [U64, U64, U64, C.POINTER(P)]),
         "eh_generate_ba": (I, [U64, U32, U64, C.POINTER(P)]),
@@ -116,6 +123,9 @@ def load(build_if_missing=True):
         "eh_similar_nodes": (I, [P, U32, C.POINTER(U64), P]),
         "eh_similar_nodes_async": (I, [P, U32, P, P]),
         "eh_intersect_rows": (I, [P, P, P, U64, P, P]),
+        "eh_symbiosity": (I, [P, P, C.c_double, C.POINTER(U64), P]),
+        "eh_symbiosity_async": (I, [P, P, C.c_double, P, P]),
+        "eh_bfs_path_length": (I, [P, U32, U64, C.POINTER(U64), C.POINTER(U64), P]),
         "eh_list_triangles": (I, [P, P, U64, P, P]),
         "eh_matrix_tune": (I, [P, P, C.POINTER(Tuning)]),
         "eh_batch_build": (I, [U32, P, U64, P, P, I, P, C.POINTER(P)]),
@@ -161,7 +171,8 @@ def _stream(stream):
 
 
 class HostGraph:
-    """The reference's MutableGraph: symmetric adjacency in CSR form on the host."""
+    """The reference's MutableGraph: symmetric adjacency in CSR form on the host,
+    or the out- and in-neighbourhoods of a directed graph."""
 
     def __init__(self, handle):
         self.h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
@@ -190,6 +201,33 @@ class HostGraph:
     def read_edge_list(cls, path):
         h = C.c_void_p()
         check(load().eh_hgraph_read_edge_list(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_directed_binary(cls, path):
+        h = C.c_void_p()
+        check(load().eh_hgraph_read_directed_binary(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_directed_edge_list(cls, path):
+        h = C.c_void_p()
+        check(load().eh_hgraph_read_directed_edge_list(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def directed_from_csr(cls, offsets, nbrs, ext_ids=None):
+        offsets = np.ascontiguousarray(offsets, np.uint64)
+        nbrs = np.ascontiguousarray(nbrs, np.uint32)
+        ext = None if ext_ids is None else np.ascontiguousarray(ext_ids, np.uint64)
+        h = C.c_void_p()
+        check(load().eh_hgraph_directed_from_csr(len(offsets) - 1, _p(offsets), _p(nbrs), _p(ext), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def directed_rmat(cls, scale, num_edges, seed, a=0.57, b=0.19, c=0.19):
+        h = C.c_void_p()
+        check(load().eh_generate_directed_rmat(scale, num_edges, a, b, c, seed, C.byref(h)))
         return cls(h)
 
     @classmethod
@@ -223,6 +261,25 @@ class HostGraph:
 
     def write_binary(self, path):
         check(load().eh_hgraph_write_binary(self.h, os.fsencode(path)))
+
+    def write_directed_binary(self, path):
+        check(load().eh_hgraph_write_directed_binary(self.h, os.fsencode(path)))
+
+    @property
+    def directed(self):
+        d = C.c_int()
+        check(load().eh_hgraph_in_view(self.h, C.byref(d), None, None, None))
+        return bool(d.value)
+
+    def in_csr(self, copy=True):
+        """(in_offsets u64[n+1], in_nbrs u32[m]): the columns (= csr() when undirected)."""
+        n = int(self.csr(copy=False)[0].shape[0] - 1)
+        d, m = C.c_int(), C.c_uint64()
+        off, nb = C.POINTER(C.c_uint64)(), C.POINTER(C.c_uint32)()
+        check(load().eh_hgraph_in_view(self.h, C.byref(d), C.byref(m), C.byref(off), C.byref(nb)))
+        o = np.ctypeslib.as_array(off, (n + 1,))
+        b = np.ctypeslib.as_array(nb, (m.value,)) if m.value else np.zeros(0, np.uint32)
+        return (o.copy(), b.copy()) if copy else (o, b)
 
     def csr(self, copy=True):
         """(offsets u64[n+1], nbrs u32[m], ext_ids u64[n], max_nbrhood_size)."""
@@ -355,6 +412,23 @@ class Matrix:
 
     def similar_nodes_async(self, threshold, d_out, stream=None):
         check(load().eh_similar_nodes_async(self.h, threshold, C.c_void_p(d_out), _stream(stream)))
+
+    def symbiosity(self, cols=None, threshold=0.5, stream=None):
+        """Rows whose out-row (this matrix) and in-row (`cols`; None = this
+        matrix, as for an undirected graph) have Jaccard ratio > threshold."""
+        c = C.c_uint64()
+        check(load().eh_symbiosity(self.h, (cols or self).h, float(threshold), C.byref(c), _stream(stream)))
+        return c.value
+
+    def symbiosity_async(self, cols, threshold, d_out, stream=None):
+        check(load().eh_symbiosity_async(self.h, (cols or self).h, float(threshold), C.c_void_p(d_out),
+                                         _stream(stream)))
+
+    def bfs(self, start, depth=0xEFFFFFF, stream=None):
+        """n_path BFS from row `start`: (path_length, vertices reached)."""
+        p, r = C.c_uint64(), C.c_uint64()
+        check(load().eh_bfs_path_length(self.h, int(start), int(depth), C.byref(p), C.byref(r), _stream(stream)))
+        return p.value, r.value
 
     def list_triangles(self, d_out, capacity, d_total, stream=None):
         check(load().eh_list_triangles(self.h, C.c_void_p(d_out), capacity, C.c_void_p(d_total),
@@ -492,6 +566,38 @@ def concat_graphs(csrs):
     return graph_rows, np.concatenate(offs), (np.concatenate(nbs) if nbs else np.zeros(0, np.uint32))
 
 
+def _splitmix_np(x):
+    """SplitMix64 output function on a u64 array (wrapping arithmetic)."""
+    with np.errstate(over="ignore"):
+        z = np.asarray(x, np.uint64) + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def orient(undirected, p_both, seed):
+    """Directed graph from an undirected one: each edge {u, v} (u < v) becomes
+    u->v and v->u with probability p_both, else one of the two with equal
+    probability, decided by SplitMix64 of (u << 32 | v) keyed by `seed`."""
+    off, nbr, _, _ = undirected.csr()
+    n = len(off) - 1
+    src = np.repeat(np.arange(n, dtype=np.uint64), np.diff(off).astype(np.int64))
+    dst = nbr.astype(np.uint64)
+    keep = src < dst
+    u, v = src[keep], dst[keep]
+    r = _splitmix_np(((u << np.uint64(32)) | v) ^ _splitmix_np(np.uint64(seed)))
+    x = (r >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    fwd = (x < p_both) | (x < p_both + (1.0 - p_both) / 2.0)
+    bwd = (x < p_both) | ~fwd
+    s_all = np.concatenate([u[fwd], v[bwd]])
+    d_all = np.concatenate([v[fwd], u[bwd]])
+    order = np.lexsort((d_all, s_all))
+    s_all, d_all = s_all[order], d_all[order]
+    offs = np.zeros(n + 1, np.uint64)
+    np.add.at(offs, s_all.astype(np.int64) + 1, 1)
+    return HostGraph.directed_from_csr(np.cumsum(offs, dtype=np.uint64), d_all.astype(np.uint32))
+
+
 def graph(kind, seed, **kw):
     """Seeded, degree-ordered generator graph -> HostGraph."""
     if kind == "rmat":
@@ -504,6 +610,14 @@ def graph(kind, seed, **kw):
     elif kind == "planted":
         g = HostGraph.planted_cliques(kw["n"], kw["edges"], kw["cliques"], kw["min_size"],
                                       kw["max_size"], seed)
+    elif kind == "recip":
+        # Directed: a degree-ordered undirected generator graph, oriented by orient().
+        base = graph(kw["base"], seed, **kw["base_params"])
+        return orient(base, kw["p_both"], seed)
+    elif kind == "drmat":
+        # Directed graphs keep their generated ids (degree reordering is undirected-only).
+        return HostGraph.directed_rmat(kw["scale"], kw["edges"], seed, kw.get("a", 0.57), kw.get("b", 0.19),
+                                       kw.get("c", 0.19))
     else:
         raise ValueError(kind)
     return g.reorder_by_degree()

@@ -264,8 +264,7 @@ __global__ void k_unit_fill(const uint32_t* __restrict__ cnt, const uint32_t* __
     for (uint32_t p = 0; p < cnt[u]; p++) units[start[u] + p] = make_uint2(u, p);
 }
 
-// similar_nodes: rows i with |row(v*) ∩ row(i)| > threshold; one warp per row,
-// each element of row(i) probed into row(v*).
+// similar_nodes: rows i with |row(v*) ∩ row(i)| > threshold; one warp per row.
 __global__ void __launch_bounds__(256) k_similar(uint64_t n, const RowDesc* __restrict__ desc,
                                                  const uint4* __restrict__ arena, uint32_t vstar,
                                                  uint32_t threshold, unsigned long long* out) {
@@ -275,16 +274,14 @@ __global__ void __launch_bounds__(256) k_similar(uint64_t n, const RowDesc* __re
   const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
   for (uint64_t r = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < n; r += nw) {
     const RowView B = load_view(desc, arena, (uint32_t)r);
-    uint32_t c = 0;
-    if (A.card && B.card) warp_for_each(B, 0xffffffffu, lane, [&](uint32_t y) { c += row_contains(A, y); });
-    c = warp_sum_u32(c);
+    const uint32_t c = warp_intersect_size(A, B, lane);
     if (lane == 0 && c > threshold) acc++;
   }
   if (lane == 0 && acc) atomicAdd(out, acc);
 }
 
-// counts[p] = |row(a[p]) ∩ row(b[p])|: the smaller row is streamed and probed
-// into the larger one.  A pair naming a row >= n gets 0xffffffff.
+// counts[p] = |row(a[p]) ∩ row(b[p])|, one warp per pair.  A pair naming a
+// row >= n gets 0xffffffff.
 __global__ void __launch_bounds__(256) k_intersect_rows(uint64_t n, const RowDesc* __restrict__ desc,
                                                         const uint4* __restrict__ arena,
                                                         const uint32_t* __restrict__ ra,
@@ -297,16 +294,7 @@ __global__ void __launch_bounds__(256) k_intersect_rows(uint64_t n, const RowDes
       if (lane == 0) counts[p] = 0xffffffffu;
       continue;
     }
-    RowView A = load_view(desc, arena, ra[p]);
-    RowView B = load_view(desc, arena, rb[p]);
-    if (A.card > B.card) {
-      const RowView T = A;
-      A = B;
-      B = T;
-    }
-    uint32_t c = 0;
-    if (A.card && B.card) warp_for_each(A, 0xffffffffu, lane, [&](uint32_t y) { c += row_contains(B, y); });
-    c = warp_sum_u32(c);
+    const uint32_t c = warp_intersect_size(load_view(desc, arena, ra[p]), load_view(desc, arena, rb[p]), lane);
     if (lane == 0) counts[p] = c;
   }
 }

@@ -178,6 +178,30 @@ __device__ inline uint64_t pshort_pair_drop(const RowView& A, const RowView& B, 
   return drop;
 }
 
+// |A ∩ B| as the reference's set_intersect reports it, the pshort ∩ pshort
+// u16 quirk included, computed by one warp; every lane returns the result.
+// Two bitsets are ANDed word by word over their common word range; otherwise
+// the smaller row is streamed and each element probed into the larger one.
+__device__ inline uint32_t warp_intersect_size(RowView A, RowView B, uint32_t lane) {
+  if (!A.card || !B.card) return 0;
+  uint32_t c = 0;
+  if (A.type == TY_BITSET && B.type == TY_BITSET) {
+    const unsigned long long* a = static_cast<const unsigned long long*>(A.p);
+    const unsigned long long* b = static_cast<const unsigned long long*>(B.p);
+    const uint32_t lo = max(A.aux, B.aux), hi = min(A.aux + A.len, B.aux + B.len);
+    for (uint32_t w = lo + lane; w < hi; w += 32) c += __popcll(a[w - A.aux] & b[w - B.aux]);
+  } else {
+    if (A.card > B.card) {
+      const RowView T = A;
+      A = B;
+      B = T;
+    }
+    warp_for_each(A, 0xffffffffu, lane, [&](uint32_t y) { c += row_contains(B, y); });
+  }
+  c = warp_sum_u32(c);
+  return c - (uint32_t)pshort_pair_drop(A, B, ~0ull);
+}
+
 // Batch mode: index g of the graph whose rows [graph_rows[g], graph_rows[g+1])
 // hold `row` (graph_rows has num_graphs + 1 ascending entries).
 __device__ __forceinline__ uint32_t graph_of(const uint32_t* graph_rows, uint32_t num_graphs, uint32_t row) {

@@ -138,6 +138,25 @@ static bool first_distinct(uint64_t target, uint64_t first_batch, Draw draw,
   return false;
 }
 
+// in-CSR of a directed graph as the transpose of its out-CSR; sources are
+// visited in ascending order, so every in-row comes out sorted.
+static void build_in_csr(HostGraph& g) {
+  const uint64_t n = g.n;
+  g.in_offsets.assign(n + 1, 0);
+  for (uint32_t v : g.nbrs) g.in_offsets[v + 1]++;
+  for (uint64_t i = 0; i < n; i++) g.in_offsets[i + 1] += g.in_offsets[i];
+  g.in_nbrs.resize(g.nbrs.size());
+  std::vector<uint64_t> at(g.in_offsets.begin(), g.in_offsets.end() - 1);
+  for (uint64_t u = 0; u < n; u++)
+    for (uint64_t e = g.offsets[u]; e < g.offsets[u + 1]; e++) g.in_nbrs[at[g.nbrs[e]]++] = (uint32_t)u;
+}
+
+static uint64_t max_row(const std::vector<uint64_t>& off) {
+  uint64_t mx = 0;
+  for (size_t i = 0; i + 1 < off.size(); i++) mx = std::max(mx, off[i + 1] - off[i]);
+  return mx;
+}
+
 static eh_status finish_graph(uint64_t n, std::vector<uint64_t>& keys, eh_hgraph_t* out) {
   HostGraph* g = new (std::nothrow) HostGraph();
   if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
@@ -310,6 +329,8 @@ eh_status eh_hgraph_read_edge_list(const char* path, eh_hgraph_t* out) {
 eh_status eh_hgraph_reorder_by_degree(eh_hgraph_t gh) {
   EH_CHECK_ARG(gh, "graph is NULL");
   HostGraph* g = HG(gh);
+  // reassign_ids (src/MutableGraph.hpp:96-123) only handles undirected graphs.
+  if (g->directed) return set_error(EH_ERR_UNSUPPORTED, "degree reordering needs an undirected graph");
   const uint64_t n = g->n;
   std::vector<uint32_t> new2old(n);
   std::iota(new2old.begin(), new2old.end(), 0);
@@ -355,6 +376,176 @@ eh_status eh_hgraph_view(eh_hgraph_t gh, uint64_t* n, uint64_t* num_edges, const
 }
 
 void eh_hgraph_free(eh_hgraph_t g) { delete HG(g); }
+
+eh_status eh_hgraph_read_directed_binary(const char* path, eh_hgraph_t* out) {
+  EH_CHECK_ARG(path && out, "path/out is NULL");
+  FILE* f = fopen(path, "rb");
+  if (!f) return set_error(EH_ERR_IO, "cannot open %s", path);
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) {
+    fclose(f);
+    return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  }
+  g->directed = true;
+  uint64_t n = 0;
+  bool ok = fread(&n, sizeof(n), 1, f) == 1 && n < (1ULL << 32);
+  if (ok) {
+    g->n = n;
+    g->offsets.assign(n + 1, 0);
+    g->in_offsets.assign(n + 1, 0);
+    g->ext_ids.resize(n);
+    for (uint64_t i = 0; i < n && ok; i++) {
+      uint64_t hdr[2], len = 0;
+      ok = fread(hdr, sizeof(uint64_t), 2, f) == 2;
+      if (!ok) break;
+      g->ext_ids[i] = hdr[0];
+      g->offsets[i + 1] = g->offsets[i] + hdr[1];
+      size_t at = g->nbrs.size();
+      g->nbrs.resize(at + hdr[1]);
+      if (hdr[1]) ok = fread(g->nbrs.data() + at, sizeof(uint32_t), hdr[1], f) == hdr[1];
+      ok = ok && fread(&len, sizeof(uint64_t), 1, f) == 1;
+      if (!ok) break;
+      g->in_offsets[i + 1] = g->in_offsets[i] + len;
+      at = g->in_nbrs.size();
+      g->in_nbrs.resize(at + len);
+      if (len) ok = fread(g->in_nbrs.data() + at, sizeof(uint32_t), len, f) == len;
+      g->max_nbrhood_size = std::max(g->max_nbrhood_size, std::max(hdr[1], len));
+    }
+  }
+  fclose(f);
+  if (ok)
+    for (uint32_t v : g->nbrs) ok = ok && v < n;
+  if (ok)
+    for (uint32_t v : g->in_nbrs) ok = ok && v < n;
+  if (!ok) {
+    delete g;
+    return set_error(EH_ERR_IO, "truncated or malformed directed binary graph %s", path);
+  }
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
+}
+
+eh_status eh_hgraph_write_directed_binary(eh_hgraph_t gh, const char* path) {
+  EH_CHECK_ARG(gh && path, "graph/path is NULL");
+  HostGraph* g = HG(gh);
+  const std::vector<uint64_t>& io = g->directed ? g->in_offsets : g->offsets;
+  const std::vector<uint32_t>& in = g->directed ? g->in_nbrs : g->nbrs;
+  FILE* f = fopen(path, "wb");
+  if (!f) return set_error(EH_ERR_IO, "cannot open %s for writing", path);
+  bool ok = fwrite(&g->n, sizeof(uint64_t), 1, f) == 1;
+  for (uint64_t i = 0; i < g->n && ok; i++) {
+    uint64_t hdr[2] = {g->ext_ids[i], g->offsets[i + 1] - g->offsets[i]};
+    ok = fwrite(hdr, sizeof(uint64_t), 2, f) == 2;
+    if (ok && hdr[1]) ok = fwrite(g->nbrs.data() + g->offsets[i], sizeof(uint32_t), hdr[1], f) == hdr[1];
+    const uint64_t len = io[i + 1] - io[i];
+    ok = ok && fwrite(&len, sizeof(uint64_t), 1, f) == 1;
+    if (ok && len) ok = fwrite(in.data() + io[i], sizeof(uint32_t), len, f) == len;
+  }
+  ok = (fclose(f) == 0) && ok;
+  return ok ? EH_OK : set_error(EH_ERR_IO, "write to %s failed", path);
+}
+
+eh_status eh_hgraph_read_directed_edge_list(const char* path, eh_hgraph_t* out) {
+  EH_CHECK_ARG(path && out, "path/out is NULL");
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return set_error(EH_ERR_IO, "cannot open %s", path);
+  std::string text((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+  std::vector<uint64_t> tok;
+  size_t p = 0, L = text.size();
+  auto is_sep = [](char c) { return c == ' ' || c == '\t' || c == '\n' || c == 'A'; };
+  while (p < L) {
+    while (p < L && is_sep(text[p])) p++;
+    if (p >= L) break;
+    size_t q = p;
+    while (q < L && !is_sep(text[q])) q++;
+    tok.push_back(strtoull(text.c_str() + p, nullptr, 10));
+    p = q;
+  }
+  if (tok.size() % 2) return set_error(EH_ERR_IO, "%s: odd number of ids", path);
+  std::unordered_map<uint64_t, uint32_t> ids;
+  std::vector<uint64_t> id_map;
+  std::vector<std::vector<uint32_t>> outs, ins;
+  auto intern = [&](uint64_t x) -> uint32_t {
+    auto it = ids.find(x);
+    if (it != ids.end()) return it->second;
+    uint32_t id = (uint32_t)id_map.size();
+    ids.emplace(x, id);
+    id_map.push_back(x);
+    outs.emplace_back();
+    ins.emplace_back();
+    return id;
+  };
+  for (size_t t = 0; t < tok.size(); t += 2) {
+    uint32_t s = intern(tok[t]);
+    uint32_t d = intern(tok[t + 1]);
+    outs[s].push_back(d);
+    ins[d].push_back(s);
+  }
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  g->directed = true;
+  g->n = outs.size();
+  auto pack = [g](std::vector<std::vector<uint32_t>>& rows, std::vector<uint64_t>& off,
+                  std::vector<uint32_t>& nbr) {
+    off.assign(g->n + 1, 0);
+    for (uint64_t i = 0; i < g->n; i++) {
+      auto& r = rows[i];
+      std::sort(r.begin(), r.end());
+      // The reference takes the maximum row size before removing duplicates.
+      g->max_nbrhood_size = std::max<uint64_t>(g->max_nbrhood_size, r.size());
+      r.erase(std::unique(r.begin(), r.end()), r.end());
+      off[i + 1] = off[i] + r.size();
+    }
+    nbr.reserve(off[g->n]);
+    for (auto& r : rows) nbr.insert(nbr.end(), r.begin(), r.end());
+  };
+  pack(ins, g->in_offsets, g->in_nbrs);
+  pack(outs, g->offsets, g->nbrs);
+  g->ext_ids = id_map;
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
+}
+
+eh_status eh_hgraph_directed_from_csr(uint64_t n, const uint64_t* offsets, const uint32_t* nbrs,
+                                      const uint64_t* ext_ids, eh_hgraph_t* out) {
+  EH_CHECK_ARG(out != nullptr, "out is NULL");
+  EH_CHECK_ARG(offsets != nullptr, "offsets is NULL");
+  EH_CHECK_ARG(n < (1ULL << 32), "n=%llu exceeds the u32 vertex id space", (unsigned long long)n);
+  EH_CHECK_ARG(offsets[0] == 0, "offsets[0] must be 0");
+  for (uint64_t i = 0; i < n; i++) {
+    EH_CHECK_ARG(offsets[i + 1] >= offsets[i], "offsets not monotone at row %llu", (unsigned long long)i);
+    for (uint64_t e = offsets[i]; e < offsets[i + 1]; e++) {
+      EH_CHECK_ARG(nbrs[e] < n, "row %llu names vertex %u >= n", (unsigned long long)i, nbrs[e]);
+      EH_CHECK_ARG(e == offsets[i] || nbrs[e] > nbrs[e - 1], "row %llu is not strictly ascending",
+                   (unsigned long long)i);
+    }
+  }
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  g->directed = true;
+  g->n = n;
+  g->offsets.assign(offsets, offsets + n + 1);
+  g->nbrs.assign(nbrs, nbrs + offsets[n]);
+  g->ext_ids.resize(n);
+  for (uint64_t i = 0; i < n; i++) g->ext_ids[i] = ext_ids ? ext_ids[i] : i;
+  eh::build_in_csr(*g);
+  g->max_nbrhood_size = std::max(eh::max_row(g->offsets), eh::max_row(g->in_offsets));
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
+}
+
+eh_status eh_hgraph_in_view(eh_hgraph_t gh, int* directed, uint64_t* num_edges, const uint64_t** in_offsets,
+                            const uint32_t** in_nbrs) {
+  EH_CHECK_ARG(gh, "graph is NULL");
+  HostGraph* g = HG(gh);
+  if (directed) *directed = g->directed ? 1 : 0;
+  const std::vector<uint64_t>& io = g->directed ? g->in_offsets : g->offsets;
+  const std::vector<uint32_t>& in = g->directed ? g->in_nbrs : g->nbrs;
+  if (num_edges) *num_edges = io[g->n];
+  if (in_offsets) *in_offsets = io.data();
+  if (in_nbrs) *in_nbrs = in.data();
+  return EH_OK;
+}
 
 eh_status eh_generate_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c,
                            uint64_t seed, eh_hgraph_t* out) {
@@ -481,6 +672,52 @@ eh_status eh_generate_planted_cliques(uint64_t n, uint64_t background_edges, uin
   __gnu_parallel::sort(keys.begin(), keys.end());
   keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
   return eh::finish_graph(n, keys, out);
+}
+
+eh_status eh_generate_directed_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c,
+                                    uint64_t seed, eh_hgraph_t* out) {
+  EH_CHECK_ARG(out, "out is NULL");
+  EH_CHECK_ARG(scale >= 1 && scale <= 31, "scale %u out of range [1,31]", scale);
+  EH_CHECK_ARG(a >= 0 && b >= 0 && c >= 0 && a + b + c <= 1.0, "bad R-MAT probabilities");
+  const uint64_t n = 1ULL << scale;
+  EH_CHECK_ARG(num_edges <= n * (n - 1), "more edges than ordered vertex pairs");
+  const double two53 = 9007199254740992.0;
+  const uint64_t t1 = (uint64_t)(a * two53), t2 = (uint64_t)((a + b) * two53),
+                 t3 = (uint64_t)((a + b + c) * two53);
+  eh::Stream st(seed, 0x44524D4154ULL /* "DRMAT" */);
+  auto draw = [&](uint64_t lo, uint64_t hi, uint64_t* dst) {
+#pragma omp parallel for schedule(static)
+    for (int64_t k = (int64_t)lo; k < (int64_t)hi; k++) {
+      uint64_t u = 0, v = 0;
+      for (uint32_t l = 0; l < scale; l++) {
+        uint64_t r = st.at((uint64_t)k * scale + l) >> 11;
+        uint64_t bu = r >= t2, bv = (r >= t1 && r < t2) || r >= t3;
+        u = (u << 1) | bu;
+        v = (v << 1) | bv;
+      }
+      dst[k - lo] = (u == v) ? eh::kSelfLoop : (u << 32) | v;
+    }
+  };
+  std::vector<uint64_t> keys;
+  if (!eh::first_distinct(num_edges, num_edges + num_edges / 2, draw, keys))
+    return set_error(EH_ERR_INVALID_ARGUMENT, "R-MAT could not reach %llu distinct edges",
+                     (unsigned long long)num_edges);
+  HostGraph* g = new (std::nothrow) HostGraph();
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  g->directed = true;
+  g->n = n;
+  g->offsets.assign(n + 1, 0);
+  g->nbrs.resize(keys.size());
+  for (uint64_t k : keys) g->offsets[(k >> 32) + 1]++;
+  for (uint64_t i = 0; i < n; i++) g->offsets[i + 1] += g->offsets[i];
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < (int64_t)keys.size(); e++) g->nbrs[e] = (uint32_t)keys[e];
+  g->ext_ids.resize(n);
+  std::iota(g->ext_ids.begin(), g->ext_ids.end(), 0);
+  eh::build_in_csr(*g);
+  g->max_nbrhood_size = std::max(eh::max_row(g->offsets), eh::max_row(g->in_offsets));
+  *out = reinterpret_cast<eh_hgraph_t>(g);
+  return EH_OK;
 }
 
 }  // extern "C"

@@ -14,13 +14,17 @@ namespace eh {
 eh_status set_error(eh_status s, const char* fmt, ...);
 void clear_error();
 
-// Host graph behind eh_hgraph_t: CSR adjacency of a symmetric graph.
+// Host graph behind eh_hgraph_t: CSR adjacency of a symmetric graph, or of
+// the out-neighbourhoods of a directed one (then with a second, in-CSR).
 struct HostGraph {
   uint64_t n = 0;
   std::vector<uint64_t> offsets;  // n+1
   std::vector<uint32_t> nbrs;     // offsets[n]
   std::vector<uint64_t> ext_ids;  // n
   uint64_t max_nbrhood_size = 0;  // as the reference reports it (pre-dedup for edge lists)
+  bool directed = false;
+  std::vector<uint64_t> in_offsets;  // directed only: n+1
+  std::vector<uint32_t> in_nbrs;     // directed only: in_offsets[n]
 };
 
 // Builds a symmetric CSR from distinct undirected keys (lo << 32 | hi, lo < hi).

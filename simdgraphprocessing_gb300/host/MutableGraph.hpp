@@ -1,6 +1,7 @@
 // Drop-in MutableGraph (the reference's src/MutableGraph.hpp:49-93): the same
 // public fields and static loaders, backed by the engine's host graph
-// (eh_hgraph_*).  Undirected graphs only (the pattern-count path).
+// (eh_hgraph_*).  Undirected graphs share one neighbourhood list for out and
+// in; directed graphs (symmetric == false) keep both.
 #ifndef EH_DROPIN_MUTABLEGRAPH_HPP
 #define EH_DROPIN_MUTABLEGRAPH_HPP
 
@@ -34,6 +35,10 @@ struct MutableGraph {
         in_edge_attributes(in_edge_attributes_in) {}
 
   ~MutableGraph() {
+    if (in_neighborhoods && in_neighborhoods != out_neighborhoods) {
+      for (auto* r : *in_neighborhoods) delete r;
+      delete in_neighborhoods;
+    }
     if (out_neighborhoods) {
       for (auto* r : *out_neighborhoods) delete r;
       delete out_neighborhoods;
@@ -41,28 +46,48 @@ struct MutableGraph {
     delete id_map;
   }
 
-  // CSR view of the adjacency (rows must be sorted ascending).
-  void to_csr(vector<uint64_t>& offsets, vector<uint32_t>& nbrs) const {
-    offsets.assign(num_nodes + 1, 0);
-    for (size_t i = 0; i < num_nodes; i++) offsets[i + 1] = offsets[i] + out_neighborhoods->at(i)->size();
-    nbrs.resize(offsets[num_nodes]);
-    for (size_t i = 0; i < num_nodes; i++) {
-      const vector<uint32_t>* r = out_neighborhoods->at(i);
+  // CSR view of a neighbourhood list (rows must be sorted ascending).
+  static void rows_to_csr(const vector<vector<uint32_t>*>* rows, size_t n, vector<uint64_t>& offsets,
+                          vector<uint32_t>& nbrs) {
+    offsets.assign(n + 1, 0);
+    for (size_t i = 0; i < n; i++) offsets[i + 1] = offsets[i] + rows->at(i)->size();
+    nbrs.resize(offsets[n]);
+    for (size_t i = 0; i < n; i++) {
+      const vector<uint32_t>* r = rows->at(i);
       if (!r->empty()) std::memcpy(&nbrs[offsets[i]], r->data(), r->size() * sizeof(uint32_t));
     }
   }
+  // The out-neighbourhoods (the rows) as CSR.
+  void to_csr(vector<uint64_t>& offsets, vector<uint32_t>& nbrs) const {
+    rows_to_csr(out_neighborhoods, num_nodes, offsets, nbrs);
+  }
+  // The in-neighbourhoods (the columns) as CSR.
+  void to_in_csr(vector<uint64_t>& offsets, vector<uint32_t>& nbrs) const {
+    rows_to_csr(in_neighborhoods, num_nodes, offsets, nbrs);
+  }
+
+  static vector<vector<uint32_t>*>* rows_of(uint64_t n, const uint64_t* off, const uint32_t* nbr) {
+    auto* rows = new vector<vector<uint32_t>*>(n);
+    for (uint64_t i = 0; i < n; i++) (*rows)[i] = new vector<uint32_t>(nbr + off[i], nbr + off[i + 1]);
+    return rows;
+  }
 
   static MutableGraph* from_hgraph(eh_hgraph_t h) {
-    uint64_t n = 0, m = 0, mx = 0;
+    uint64_t n = 0, m = 0, mx = 0, in_m = 0;
     const uint64_t* off = nullptr;
     const uint32_t* nbr = nullptr;
     const uint64_t* ext = nullptr;
+    const uint64_t* ioff = nullptr;
+    const uint32_t* inbr = nullptr;
+    int directed = 0;
     common::check(eh_hgraph_view(h, &n, &m, &off, &nbr, &ext, &mx));
+    common::check(eh_hgraph_in_view(h, &directed, &in_m, &ioff, &inbr));
     auto* ids = new vector<uint64_t>(ext, ext + n);
-    auto* rows = new vector<vector<uint32_t>*>(n);
-    for (uint64_t i = 0; i < n; i++) (*rows)[i] = new vector<uint32_t>(nbr + off[i], nbr + off[i + 1]);
+    auto* rows = rows_of(n, off, nbr);
+    auto* cols = directed ? rows_of(n, ioff, inbr) : rows;
     eh_hgraph_free(h);
-    return new MutableGraph(n, m, mx, true, ids, nullptr, rows, rows, nullptr, nullptr);
+    // The reference's directed loaders count out and in entries (MutableGraph.hpp:675-688).
+    return new MutableGraph(n, directed ? m + in_m : m, mx, !directed, ids, nullptr, rows, cols, nullptr, nullptr);
   }
 
   eh_hgraph_t to_hgraph() const {
@@ -92,6 +117,35 @@ struct MutableGraph {
     eh_status s = eh_hgraph_write_binary(h, path.c_str());
     eh_hgraph_free(h);
     common::check(s);
+  }
+  // MutableGraph::directedFromBinary (src/MutableGraph.hpp:656-714).
+  static MutableGraph* directedFromBinary(const string path) {
+    eh_hgraph_t h = nullptr;
+    common::check(eh_hgraph_read_directed_binary(path.c_str(), &h));
+    return from_hgraph(h);
+  }
+  // MutableGraph::directedFromEdgeList (src/MutableGraph.hpp:893-986).
+  static MutableGraph* directedFromEdgeList(const string path) {
+    eh_hgraph_t h = nullptr;
+    common::check(eh_hgraph_read_directed_edge_list(path.c_str(), &h));
+    return from_hgraph(h);
+  }
+  // MutableGraph::writeDirectedToBinary (src/MutableGraph.hpp:634-654): per node
+  // u64 external id, size_t out length, out ids, size_t in length, in ids.
+  void writeDirectedToBinary(const string path) {
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot open " + path + " for writing");
+    bool ok = fwrite(&num_nodes, sizeof(size_t), 1, f) == 1;
+    for (size_t i = 0; i < num_nodes && ok; i++) {
+      ok = fwrite(&id_map->at(i), sizeof(uint64_t), 1, f) == 1;
+      for (const vector<uint32_t>* r : {out_neighborhoods->at(i), in_neighborhoods->at(i)}) {
+        const size_t len = r->size();
+        ok = ok && fwrite(&len, sizeof(size_t), 1, f) == 1;
+        if (ok && len) ok = fwrite(r->data(), sizeof(uint32_t), len, f) == len;
+      }
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) throw std::runtime_error("write to " + path + " failed");
   }
   // MutableGraph::reorder_by_degree (src/MutableGraph.hpp:268-272).
   void reorder_by_degree() {

@@ -29,3 +29,55 @@ def generate(eh, spec):
     off, nbr, _, _ = g.csr()
     assert csr_sha(off, nbr) == spec["csr_sha256"], "generator drifted from the fixture graph"
     return off, nbr
+
+
+DIRECTED_FIXTURE = os.path.join(HERE, "golden", "reference_directed.json")
+
+
+def load_directed():
+    with open(DIRECTED_FIXTURE) as f:
+        return json.load(f)
+
+
+def directed_graphs():
+    return load_directed()["graphs"]
+
+
+def directed_sha(g):
+    off, nbr, _, _ = g.csr()
+    ioff, inbr = g.in_csr()
+    h = hashlib.sha256()
+    for a, t in ((off, "<u8"), (nbr, "<u4"), (ioff, "<u8"), (inbr, "<u4")):
+        h.update(a.astype(t).tobytes())
+    return h.hexdigest()
+
+
+def generate_directed(eh, spec):
+    """(out_off, out_nbr, in_off, in_nbr) of a directed fixture graph."""
+    g = eh.graph(spec["kind"], spec["seed"], **spec["params"])
+    assert directed_sha(g) == spec["sha256"], "generator drifted from the fixture graph"
+    off, nbr, _, _ = g.csr()
+    ioff, inbr = g.in_csr()
+    return off, nbr, ioff, inbr
+
+
+def full_block_directed():
+    """Directed (out_off, out_nbr): vertex h = 65536 with out- and in-edges to
+    every vertex of [0, 65536), so out(h) and in(h) each fill the 2^16 block 0."""
+    import numpy as np
+    h = 65536
+    off = np.zeros(h + 2, np.uint64)
+    off[1:h + 1] = np.arange(1, h + 1)
+    off[h + 1] = 2 * h
+    nbr = np.concatenate([np.full(h, h, np.uint32), np.arange(h, dtype=np.uint32)])
+    return off, nbr
+
+
+def full_block_undirected():
+    """Symmetric (off, nbr): rows 65536 and 65537 both adjacent to all of [0, 65536)."""
+    import numpy as np
+    deg = np.concatenate([np.full(65536, 2), [65536, 65536]]).astype(np.uint64)
+    off = np.concatenate([[0], np.cumsum(deg)]).astype(np.uint64)
+    nbr = np.concatenate([np.tile(np.array([65536, 65537], np.uint32), 65536),
+                          np.arange(65536, dtype=np.uint32), np.arange(65536, dtype=np.uint32)])
+    return off, nbr

@@ -9,8 +9,10 @@ the reference's binary format, and records:
     layout and edge selection, for byte-format parity;
   * a SHA-256 of the generated CSR, so that a host that regenerates the graph
     (x86-64 or aarch64) can prove it got the same input.
+With --directed it writes tests/golden/reference_directed.json instead: the
+symbiosity and n_path apps on seeded directed graphs (directed binary format).
 Needs an x86-64 host with the reference tree (the reference uses SSE/AVX).
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--directed]
 """
 import hashlib
 import json
@@ -28,6 +30,7 @@ import simdgraphprocessing_gb300 as eh  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref")
 OUT = os.path.join(HERE, "reference_counts.json")
+OUT_DIRECTED = os.path.join(HERE, "reference_directed.json")
 
 GRAPHS = [
     {"name": "rmat_s10", "kind": "rmat", "seed": 101, "params": {"scale": 10, "edges": 8000}},
@@ -50,6 +53,74 @@ APPS = {
 }
 
 
+# Graphs for the directed apps (symbiosity, n_path), written in the directed
+# binary format and run with --asymmetric; "undirected" entries use the
+# undirected format and loader.
+DIRECTED = [
+    {"name": "drmat_s10", "kind": "drmat", "seed": 201, "params": {"scale": 10, "edges": 6000}},
+    {"name": "drmat_s13", "kind": "drmat", "seed": 202, "params": {"scale": 13, "edges": 80000}},
+    {"name": "recip_rmat_s12", "kind": "recip", "seed": 203,
+     "params": {"base": "rmat", "base_params": {"scale": 12, "edges": 50000}, "p_both": 0.5}},
+    {"name": "recip_er_3000", "kind": "recip", "seed": 204,
+     "params": {"base": "er", "base_params": {"n": 3000, "edges": 30000}, "p_both": 0.7}},
+    # Rows longer than 4,096 entries (the GPU BFS splits those over the grid).
+    {"name": "recip_rmat_s15", "kind": "recip", "seed": 205,
+     "params": {"base": "rmat", "base_params": {"scale": 15, "edges": 1000000}, "p_both": 0.6}},
+    {"name": "rmat_s12_undirected", "kind": "rmat", "seed": 102, "params": {"scale": 12, "edges": 50000},
+     "undirected": True},
+]
+NPATH_START, NPATH_DEPTH = 7, 2
+
+
+def directed_sha(g):
+    off, nbr, _, _ = g.csr()
+    ioff, inbr = g.in_csr()
+    h = hashlib.sha256()
+    for a, t in ((off, "<u8"), (nbr, "<u4"), (ioff, "<u8"), (inbr, "<u4")):
+        h.update(a.astype(t).tobytes())
+    return h.hexdigest()
+
+
+def run_directed(binary, graph, layout, undirected, extra=()):
+    args = [os.path.join(REF, binary), "--graph=" + graph, "--input_type=binary", "--t=4", "--layout=" + layout]
+    if not undirected:
+        args.append("--asymmetric")
+    return subprocess.run(args + list(extra), stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                          check=True).stdout
+
+
+def make_directed(td):
+    entries = []
+    for spec in DIRECTED:
+        g = eh.graph(spec["kind"], spec["seed"], **spec["params"])
+        path = os.path.join(td, spec["name"] + ".dbin")
+        und = spec.get("undirected", False)
+        if und:
+            g.write_binary(path)
+        else:
+            g.write_directed_binary(path)
+        e = dict(spec)
+        off, nbr, _, _ = g.csr()
+        e["n"] = int(len(off) - 1)
+        e["out_entries"] = int(len(nbr))
+        e["sha256"] = directed_sha(g)
+        e["counts"] = {}
+        for layout in LAYOUTS:
+            c = {}
+            out = run_directed("symbiosity", path, layout, und)
+            c["symbiosity"] = int(re.search(r"Count:\s*(\d+)", out).group(1))
+            out = run_directed("n_path", path, layout, und)
+            c["n_path_start"] = int(re.search(r"Internal:\s*(\d+)", out).group(1))
+            c["n_path"] = int(re.search(r"path length:\s*(\d+)", out).group(1))
+            out = run_directed("n_path", path, layout, und,
+                               ("--start_node=%d" % NPATH_START, "--n=%d" % NPATH_DEPTH))
+            c["n_path_s%d_d%d" % (NPATH_START, NPATH_DEPTH)] = int(re.search(r"path length:\s*(\d+)", out).group(1))
+            e["counts"][layout] = c
+        print(spec["name"], e["counts"]["hybrid"], flush=True)
+        entries.append(e)
+    return entries
+
+
 def csr_sha(off, nbr):
     h = hashlib.sha256()
     h.update(off.astype("<u8").tobytes())
@@ -64,10 +135,53 @@ def run_app(binary, graph, layout):
     return out
 
 
+def full_block_quirks(td):
+    """The pshort u16 partition-count quirk (intersection.hpp:857-865) as the
+    reference binaries show it on the two full-block graphs of tests/_golden.py."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import _golden
+    out = {"symbiosity_full_block": {}, "similar_nodes_full_block": {}}
+    off, nbr = _golden.full_block_directed()
+    dpath = os.path.join(td, "full_block.dbin")
+    eh.HostGraph.directed_from_csr(off, nbr).write_directed_binary(dpath)
+    off, nbr = _golden.full_block_undirected()
+    upath = os.path.join(td, "full_block.bin")
+    eh.HostGraph.from_csr(off, nbr).write_binary(upath)
+    for layout in LAYOUTS:
+        o = run_directed("symbiosity", dpath, layout, False)
+        out["symbiosity_full_block"][layout] = int(re.search(r"Count:\s*(\d+)", o).group(1))
+        o = run_app("similar_nodes", upath, layout)
+        out["similar_nodes_full_block"][layout] = int(re.search(r"Count:\s*(\d+)", o).group(1))
+    return out
+
+
+def main_directed():
+    with tempfile.TemporaryDirectory() as td:
+        entries = make_directed(td)
+        quirks = full_block_quirks(td)
+    doc = {
+        "generated_by": "tests/golden/make_golden.py --directed",
+        "reference_binaries": "oracle/build_ref.sh (unmodified reference sources): apps symbiosity, n_path",
+        "reference_gtest_goldens": {
+            "source": "reference test/symbiosity_test.cpp, test/n_path_test.cpp",
+            "symbiosity_dfacebook_hybrid": 0, "symbiosity_facebook_hybrid": 4039,
+            "n_path_dfacebook_uint_start0_n4": 4,
+        },
+        "n_path_start": NPATH_START, "n_path_depth": NPATH_DEPTH,
+        "graphs": entries,
+        "quirks": quirks,
+    }
+    with open(OUT_DIRECTED, "w") as f:
+        json.dump(doc, f, indent=1, sort_keys=True)
+    print("wrote", OUT_DIRECTED)
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "ref_rowdump")):
         sys.exit("oracle/_ref is not built; run: sh oracle/build_ref.sh /root/reference")
     eh.load()
+    if "--directed" in sys.argv:
+        return main_directed()
     entries = []
     with tempfile.TemporaryDirectory() as td:
         for spec in GRAPHS:

@@ -18,7 +18,7 @@ HOST = os.path.join(ROOT, "simdgraphprocessing_gb300", "host")
 APPS = os.path.join(ROOT, "simdgraphprocessing_gb300", "apps")
 CUDA_INC = "/usr/local/cuda/include"
 REF_TESTS = ["undirected_triangle_counting_test", "n_clique_test", "undirected_lollipop_counting_test",
-             "similar_nodes_test"]
+             "similar_nodes_test", "symbiosity_test", "n_path_test"]
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(_golden.REFERENCE_TREE, "test")),
@@ -33,11 +33,11 @@ def test_reference_gtests_compile_against_dropin_headers(name):
     assert r.returncode == 0, r.stdout[-3000:]
 
 
-def _build_driver(tmp_path, eh):
-    exe = str(tmp_path / "dropin_apps")
+def _build_driver(tmp_path, eh, name="dropin_apps"):
+    exe = str(tmp_path / name)
     libdir = os.path.dirname(eh.lib_path())
     cmd = ["g++", "-std=c++11", "-O2", "-fopenmp", "-I", HOST, "-I", APPS, "-I", CUDA_INC,
-           os.path.join(ROOT, "tests", "cpp", "dropin_apps.cpp"), "-o", exe,
+           os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-o", exe,
            "-L", libdir, "-leh_gb300", "-Wl,-rpath," + libdir, "-L/usr/local/cuda/lib64", "-lcudart"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     assert r.returncode == 0, r.stdout[-3000:]
@@ -46,6 +46,30 @@ def _build_driver(tmp_path, eh):
 
 def test_dropin_driver_compiles(tmp_path, eh):
     _build_driver(tmp_path, eh)
+    _build_driver(tmp_path, eh, "dropin_directed")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layout", ["hybrid", "uint", "bs", "pshort"])
+def test_dropin_directed_apps_reproduce_reference(tmp_path, eh, layout):
+    exe = _build_driver(tmp_path, eh, "dropin_directed")
+    doc = _golden.load_directed()
+    start, depth = doc["n_path_start"], doc["n_path_depth"]
+    for spec in doc["graphs"]:
+        g = eh.graph(spec["kind"], spec["seed"], **spec["params"])
+        assert _golden.directed_sha(g) == spec["sha256"]
+        path = str(tmp_path / (spec["name"] + ".bin"))
+        directed = not spec.get("undirected", False)
+        if directed:
+            g.write_directed_binary(path)
+        else:
+            g.write_binary(path)
+        want = spec["counts"][layout]
+        args = [exe, path, layout, str(int(directed)), str(want["symbiosity"]), str(want["n_path"]), str(start),
+                str(depth), str(want["n_path_s%d_d%d" % (start, depth)])]
+        r = subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        assert r.returncode == 0, (spec["name"], r.stdout[-2000:])
+        assert "Start node - External: %d Internal: %d" % (want["n_path_start"], want["n_path_start"]) in r.stdout
 
 
 @pytest.mark.gpu
