@@ -168,8 +168,8 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
       }
     };
     const Shape start = best;
-    for (uint32_t co : {0u, 8192u, 16384u})
-      if (co != start.core) consider(Shape{start.light_max, start.unit_span, start.ctas, co});
+    for (uint32_t co : {0u, 16384u, 32768u, 65536u, 98304u, 131072u})
+      if (co != start.core && co <= kCoreMaxK) consider(Shape{start.light_max, start.unit_span, start.ctas, co});
     const Shape after_core = best;
     for (int c = 1; c <= cmax; c++)
       if ((uint32_t)c != after_core.ctas)
@@ -179,7 +179,7 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
       if (lm != after_ctas.light_max && lm <= kLightMax)
         consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas, after_ctas.core});
     const Shape after_lm = best;
-    for (uint32_t us : {32u, 64u, 128u, 256u, 512u})
+    for (uint32_t us : {32u, 128u, 256u, 512u, 1024u, 2048u})
       if (us != after_lm.unit_span) consider(Shape{after_lm.light_max, us, after_lm.ctas, after_lm.core});
     if (s == EH_OK) {
       s = apply_shape(m, best, st);

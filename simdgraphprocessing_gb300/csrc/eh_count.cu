@@ -25,6 +25,7 @@
 // Per-lane counts stay in registers; one u64 atomic per CTA at the end replaces
 // the reference's per-thread padded t_count array.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "eh_kernels.cuh"
@@ -36,14 +37,27 @@ namespace {
 constexpr int NWARPS = kCtaThreads / 32;
 constexpr uint32_t kLightChunk = 16;  // light pivots per atomic grab
 
-struct __align__(16) PivotSmem {
+struct __align__(16) HeavySmem {
   unsigned long long words[kCtaWordCap];
-  unsigned long long abits[kCoreMaxK / 64];  // pivot ∩ [0, core_k) as bits
+  unsigned long long abits[kCoreAndMax / 64];  // pivot ∩ [0, min(core_k, kCoreAndMax)) as bits
   uint32_t list[kCtaListCap];
-  uint32_t wlist[NWARPS][kLightMax];
   uint32_t scan[kCtaThreads];
   uint32_t unit;
 };
+
+// Warp, CTA, then one u64 atomic per CTA into the single count.
+__device__ __forceinline__ void cta_add(unsigned long long acc, const PivotArgs& a) {
+  __shared__ unsigned long long s_red[NWARPS];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  acc = warp_sum_u64(acc);
+  if (lane == 0) s_red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < NWARPS; w++) tot += s_red[w];
+    if (tot && !a.graph_rows) atomicAdd(a.out, tot);
+  }
+}
 
 __device__ __forceinline__ uint32_t ilog2p1(uint32_t x) { return 32u - __clz(x | 1u); }
 
@@ -90,12 +104,12 @@ __device__ uint32_t pair_count_warp(const uint32_t* L, uint32_t e, const RowView
   return warp_sum_u32(c);
 }
 
+// Heavy pivots: 6 resident CTAs per SM, 40 registers per thread (the per-pair
+// choice keeps many values live, and at 32 registers it spilled).
 template <bool LOLLI>
-// 8 resident CTAs per SM (64 warps, 32 registers per thread): the kernel is
-// bound by the latency of scattered probes, so occupancy pays.
-__global__ void __launch_bounds__(kCtaThreads, 8) k_pivots(PivotArgs a, const uint2* __restrict__ units,
-                                                        uint32_t n_units) {
-  __shared__ PivotSmem s;
+__global__ void __launch_bounds__(kCtaThreads, 6) k_pivots_heavy(PivotArgs a, const uint2* __restrict__ units,
+                                                              uint32_t n_units) {
+  __shared__ HeavySmem s;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long acc = 0;
 
@@ -123,12 +137,13 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots(PivotArgs a, const ui
     // The core path is skipped for pshort pivots of >= 65,536 entries, where the
     // reference's u16 partition count can drop a block (see pshort_pair_drop).
     const bool use_core = a.core_k && !(A.type == TY_PSHORT && A.card >= 65536u);
+    const uint32_t and_k = min(a.core_k, kCoreAndMax);
     if (use_core) {
-      for (uint32_t k = threadIdx.x; k < (a.core_k >> 6); k += kCtaThreads) s.abits[k] = 0ull;
+      for (uint32_t k = threadIdx.x; k < (and_k >> 6); k += kCtaThreads) s.abits[k] = 0ull;
       __syncthreads();
       for (uint32_t k = threadIdx.x; k < A.card; k += kCtaThreads) {
         const uint32_t x = L[k];
-        if (x < a.core_k) atomicOr(&s.abits[x >> 6], 1ull << (x & 63));
+        if (x < and_k) atomicOr(&s.abits[x >> 6], 1ull << (x & 63));
       }
     }
     __syncthreads();
@@ -140,12 +155,13 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots(PivotArgs a, const ui
       const uint32_t j = L[e];
       uint32_t cnt;
       if (use_core && j < a.core_k) {
-        // Core row j holds row(j) ∩ [0, j): AND it with the pivot's bits, or probe
-        // the e pivot elements below j, whichever touches fewer words.
+        // Core row j holds row(j) ∩ [0, j): AND it with the pivot's bits (j within
+        // the staged bits), or probe the e pivot elements below j, whichever
+        // touches fewer words.
         const unsigned long long* row = a.core + core_row_offset(j);
         const uint32_t wj = (j + 63) >> 6;
         cnt = 0;
-        if (wj <= 2 * e) {
+        if (j <= and_k && wj <= 2 * e) {
           for (uint32_t w = lane; w < wj; w += 32) cnt += __popcll(s.abits[w] & __ldg(row + w));
         } else {
           for (uint32_t t = lane; t < e; t += 32) {
@@ -168,9 +184,20 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots(PivotArgs a, const ui
     __syncthreads();
   }
 
+  cta_add(acc, a);
+}
+
+// Light pivots: 8 resident CTAs per SM (64 warps, 32 registers per thread):
+// bound by the latency of scattered probes, so occupancy pays.
+template <bool LOLLI>
+__global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
+  __shared__ uint32_t wlist[NWARPS][kLightMax];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long acc = 0;
+
   // ---- light pivots: one warp each, all (e, t) pairs probed in parallel ----
   const uint32_t n_light = a.n_order - a.n_heavy;
-  uint32_t* list = s.wlist[warp];
+  uint32_t* list = wlist[warp];
   for (;;) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(&a.counters[1], kLightChunk);
@@ -209,16 +236,7 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots(PivotArgs a, const ui
     }
   }
 
-  // ---- reduce: warp, CTA, one atomic ----
-  acc = warp_sum_u64(acc);
-  __shared__ unsigned long long s_red[NWARPS];
-  if (lane == 0) s_red[warp] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long tot = 0;
-    for (int w = 0; w < NWARPS; w++) tot += s_red[w];
-    if (tot && !a.graph_rows) atomicAdd(a.out, tot);
-  }
+  cta_add(acc, a);
 }
 
 // Dense core build: one warp per row j < core_k writes row(j) ∩ [0, j) as bits.
@@ -301,13 +319,23 @@ __global__ void __launch_bounds__(256) k_intersect_rows(uint64_t n, const RowDes
 
 }  // namespace
 
-int pivot_grid(int device) {
+// Persistent grid sizes per device: SMs x resident CTAs of the light kernel
+// (the tunable grid) and of the heavy kernel (its cap), looked up once.
+static int grid_of(int device, bool heavy) {
+  static std::atomic<int> cache[64][2];
+  if (device < 0 || device >= 64) return 152;
+  int g = cache[device][heavy].load();
+  if (g > 0) return g;
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pivots<false>, kCtaThreads, 0);
-  if (per < 1) per = 1;
-  return sms * per;
+  if (heavy) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pivots_heavy<false>, kCtaThreads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pivots_light<false>, kCtaThreads, 0);
+  g = std::max(1, sms) * std::max(1, per);
+  cache[device][heavy].store(g);
+  return g;
 }
+
+int pivot_grid(int device) { return grid_of(device, false); }
 
 template <bool LOLLI>
 static cudaError_t launch_pivots(const PivotArgs& a, const uint2* units, uint32_t n_units, int grid,
@@ -316,7 +344,13 @@ static cudaError_t launch_pivots(const PivotArgs& a, const uint2* units, uint32_
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(a.out, 0, sizeof(unsigned long long) * (a.graph_rows ? a.num_graphs : 1), st);
   if (e != cudaSuccess) return e;
-  k_pivots<LOLLI><<<grid, kCtaThreads, 0, st>>>(a, units, n_units);
+  int device = 0;
+  if ((e = cudaGetDevice(&device)) != cudaSuccess) return e;
+  if (n_units) {
+    const int gh = std::min(grid, grid_of(device, true));
+    k_pivots_heavy<LOLLI><<<std::max(gh, 1), kCtaThreads, 0, st>>>(a, units, n_units);
+  }
+  if (a.n_order > a.n_heavy) k_pivots_light<LOLLI><<<std::max(grid, 1), kCtaThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 

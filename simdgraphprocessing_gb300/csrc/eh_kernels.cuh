@@ -94,7 +94,11 @@ int pivot_grid(int device);  // persistent grid: SMs x resident CTAs of the pivo
 // Dense core: for every row j < core_k, the bits of row(j) ∩ [0, j) packed in
 // ceil(j/64) words starting at word core_row_offset(j) (a lower-triangular
 // bitmap of the highest-degree rows, which degree ordering puts first).
-constexpr uint32_t kCoreMaxK = 24576;  // 37.7 MB of bits
+constexpr uint32_t kCoreMaxK = 131072;     // 1.07 GB of bits, the tuner's largest core
+constexpr uint32_t kCoreDefaultK = 65536;  // 268 MB: the core of a matrix the tuner has not seen
+// Heavy pivots keep their elements below min(core_k, kCoreAndMax) as bits in
+// shared memory, to AND with core rows in that range.
+constexpr uint32_t kCoreAndMax = 65536;
 __host__ __device__ inline uint64_t core_row_offset(uint32_t j) {
   if (j == 0) return 0;
   const uint64_t a = (uint64_t)(j - 1) >> 6, b = (uint64_t)(j - 1) & 63;

@@ -65,7 +65,7 @@ struct Matrix {
   // Work-shape parameters of the pivot kernel (set by the autotuner).
   uint32_t light_max = kDefaultLightMax;
   uint32_t unit_span = kDefaultUnitSpan;
-  uint32_t core_limit = kCoreMaxK;  // rows in the dense core at most (0 = no core)
+  uint32_t core_limit = kCoreDefaultK;  // rows in the dense core at most (0 = no core)
   bool is_batch = false;            // the union matrix of an eh_batch_t
 };
 
