@@ -335,14 +335,19 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
     }
     CU(launch_clique_cta(a, 0, nG, w.counters + 2, cmax, w.clique_scratch, grid, st), "clique kernel (global)");
   }
-  if (nB > nG) {
-    const uint32_t cmax = p.largest_at_most(kCliqueSmemMax);
-    const int grid = (int)std::min<uint64_t>(nB - nG, 4ull * sms);
-    CU(launch_clique_cta(a, nG, nB, w.counters + 3, cmax, nullptr, grid, st), "clique kernel (shared)");
+  // The shared-memory tier runs in size bands, each launch sized for its own
+  // largest pivot, so that the many small pivots are not held to the
+  // occupancy of the largest one.
+  static const uint32_t bands[] = {kCliqueSmemMax, 512, 256, 128, 32};
+  for (int b = 0; b + 1 < (int)(sizeof(bands) / sizeof(bands[0])); b++) {
+    const uint32_t p0 = p.above(bands[b]), p1 = p.above(bands[b + 1]);
+    if (p1 <= p0) continue;
+    const uint32_t cmax = p.largest_at_most(bands[b]);
+    CU(launch_clique_cta(a, p0, p1, w.counters + 3 + b, cmax, nullptr, 0, st), "clique kernel (shared)");
   }
   if (nL > nB) {
     const int grid = (int)std::min<uint64_t>((nL - nB + 63) / 64, 8ull * sms);
-    CU(launch_clique_light(a, nB, nL, w.counters + 4, grid > 0 ? grid : 1, st), "clique kernel (warp)");
+    CU(launch_clique_light(a, nB, nL, w.counters + 7, grid > 0 ? grid : 1, st), "clique kernel (warp)");
   }
   return EH_OK;
 }

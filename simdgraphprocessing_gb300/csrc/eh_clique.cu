@@ -18,7 +18,10 @@
 // one-word masks (|A_i| <= 32); one CTA per pivot with masks in shared memory
 // (|A_i| <= kCliqueSmemMax); one CTA per pivot with masks in a global scratch
 // slot (larger pivots).
+#include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
 #include <cstdint>
 
 #include "eh_kernels.cuh"
@@ -286,6 +289,23 @@ uint64_t clique_slot_words(uint32_t cmax, uint32_t k) {
   return (uint64_t)cmax + (uint64_t)cmax * W + (uint64_t)NW * 2 * (k - 2) * W;
 }
 
+// SMs x resident CTAs of the shared-memory clique kernel with `bytes` of
+// dynamic shared memory; looked up once per (device, size), so that launches
+// captured into a CUDA graph after a direct run make no occupancy query.
+static int resident_ctas(int dev, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, size_t>, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find({dev, bytes});
+  if (it != cache.end()) return it->second;
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clique_cta<false>, kCtaThreads, bytes);
+  const int g = std::max(sms, 1) * std::max(per, 1);
+  cache[{dev, bytes}] = g;
+  return g;
+}
+
 cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                                 int grid, cudaStream_t st) {
   if (pos_end <= pos_begin) return cudaSuccess;
@@ -314,6 +334,9 @@ cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t 
       int prev = set_bytes[dev].load();
       while ((int)bytes > prev && !set_bytes[dev].compare_exchange_weak(prev, (int)bytes)) {
       }
+    }
+    if (grid <= 0) {  // fill the GPU: SMs x resident CTAs at this shared-memory size, at most one per pivot
+      grid = (int)std::min<uint64_t>(pos_end - pos_begin, (uint64_t)resident_ctas(dev, bytes));
     }
     k_clique_cta<false><<<grid, kCtaThreads, bytes, st>>>(a, pos_begin, pos_end, counter, cmax, W, nullptr, slot);
   }

@@ -36,6 +36,7 @@ namespace {
 
 constexpr int NWARPS = kCtaThreads / 32;
 constexpr uint32_t kLightChunk = 16;  // light pivots per atomic grab
+constexpr uint32_t kStreamMinE = 256;  // core rows: consider streaming row(j) only past this many probes
 
 struct __align__(16) HeavySmem {
   unsigned long long words[kCtaWordCap];
@@ -104,6 +105,23 @@ __device__ uint32_t pair_count_warp(const uint32_t* L, uint32_t e, const RowView
   return warp_sum_u32(c);
 }
 
+// Per-lane part of |{t < e : L[t] in B}| by streaming B's elements below j and
+// looking each up in the pivot (a bit test for a bitset pivot, else a binary
+// search of L[0, e)); the caller sums over the warp.
+__device__ __forceinline__ uint32_t pair_count_stream(const uint32_t* L, uint32_t e, const RowView& A,
+                                                      const RowView& B, uint32_t j, uint32_t lane) {
+  uint32_t c = 0;
+  if (A.type == TY_BITSET) {
+    warp_for_each(B, j, lane, [&](uint32_t y) { c += row_contains(A, y); });
+  } else {
+    warp_for_each(B, j, lane, [&](uint32_t y) {
+      const uint32_t p = lower_bound_u32(L, 0, e, y);
+      c += (p < e && L[p] == y);
+    });
+  }
+  return c;
+}
+
 // Heavy pivots: 6 resident CTAs per SM, 40 registers per thread (the per-pair
 // choice keeps many values live, and at 32 registers it spilled).
 template <bool LOLLI>
@@ -155,18 +173,30 @@ __global__ void __launch_bounds__(kCtaThreads, 6) k_pivots_heavy(PivotArgs a, co
       const uint32_t j = L[e];
       uint32_t cnt;
       if (use_core && j < a.core_k) {
-        // Core row j holds row(j) ∩ [0, j): AND it with the pivot's bits (j within
-        // the staged bits), or probe the e pivot elements below j, whichever
-        // touches fewer words.
+        // Core row j holds row(j) ∩ [0, j).  Cheapest of: AND it with the pivot's
+        // bits (j within the staged bits; wj words), probe it at the e pivot
+        // elements below j (e words), or stream row(j) itself and look each
+        // element up in the pivot (|row(j)| lookups; rows past the highest-degree
+        // ones are short while e grows with the pivot).
         const unsigned long long* row = a.core + core_row_offset(j);
         const uint32_t wj = (j + 63) >> 6;
         cnt = 0;
-        if (j <= and_k && wj <= 2 * e) {
+        if (j <= and_k && wj <= e) {
           for (uint32_t w = lane; w < wj; w += 32) cnt += __popcll(s.abits[w] & __ldg(row + w));
         } else {
-          for (uint32_t t = lane; t < e; t += 32) {
-            const uint32_t x = L[t];
-            cnt += (uint32_t)((__ldg(row + (x >> 6)) >> (x & 63)) & 1ull);
+          bool stream = false;
+          RowView B;
+          if (e > kStreamMinE) {
+            B = load_view(a.desc, a.arena, j);
+            stream = (uint64_t)B.card * (A.type == TY_BITSET ? 1u : ilog2p1(e)) < e;
+          }
+          if (stream) {
+            cnt = pair_count_stream(L, e, A, B, j, lane);
+          } else {
+            for (uint32_t t = lane; t < e; t += 32) {
+              const uint32_t x = L[t];
+              cnt += (uint32_t)((__ldg(row + (x >> 6)) >> (x & 63)) & 1ull);
+            }
           }
         }
         cnt = warp_sum_u32(cnt);

@@ -130,7 +130,8 @@ constexpr uint32_t kCliqueSmemMax = 1024;  // pivots up to this size keep their 
 uint64_t clique_slot_words(uint32_t cmax, uint32_t k);
 cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                                 int grid, cudaStream_t st);
-// gscratch == nullptr: masks in dynamic shared memory; else grid slots of
+// gscratch == nullptr: masks in dynamic shared memory (grid <= 0: as many CTAs
+// as fit on the GPU, at most one per pivot); else grid slots of
 // clique_slot_words(cmax, k) words each in global memory.
 cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                               uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st);
