@@ -100,11 +100,12 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   m->arena_units = m->tot.payload_units;
   if ((e = cudaMalloc((void**)&m->desc, nn * sizeof(RowDesc))) != cudaSuccess ||
       (e = cudaMalloc((void**)&m->arena, (m->arena_units + 1) * 16)) != cudaSuccess ||
-      (e = cudaMalloc((void**)&m->counters, 64)) != cudaSuccess)
+      (e = cudaMalloc((void**)&m->counters, 128)) != cudaSuccess)
     return fail(set_error(EH_ERR_OUT_OF_MEMORY, "matrix allocation (%llu bytes) failed: %s",
                           (unsigned long long)((m->arena_units + 1) * 16 + nn * 16), cudaGetErrorString(e)));
-  m->result = reinterpret_cast<unsigned long long*>(m->counters + 8);
-  m->device_bytes = nn * sizeof(RowDesc) + (m->arena_units + 1) * 16 + 64;
+  // Words 0..15: work-queue counters; 16..17: the u64 result of the synchronous calls.
+  m->result = reinterpret_cast<unsigned long long*>(m->counters + 16);
+  m->device_bytes = nn * sizeof(RowDesc) + (m->arena_units + 1) * 16 + 128;
   cudaMemsetAsync(m->arena, 0, (m->arena_units + 1) * 16, st);
   if ((e = launch_encode(n, d_off, d_nbr, d_mask, sel, meas, off16, m->desc, m->arena, st)) != cudaSuccess)
     return fail(cuda_fail(e, "encode kernel"));
@@ -307,11 +308,12 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
   eh_status s = ensure_plan(m, st);
   if (s != EH_OK) return s;
   const Plan& p = m->plan;
-  const uint32_t nG = p.above(kCliqueSmemMax);
+  const uint32_t cap = clique_smem_cap(k, m->device);
+  const uint32_t nG = p.above(cap);
   const uint32_t nB = p.above(32);
   const uint32_t nL = p.above(k - 2);
   CliqueArgs a{m->desc, m->arena, p.order, k, out, graph_rows, num_graphs, p.core, p.core_k};
-  CU(cudaMemsetAsync(w.counters, 0, 8 * sizeof(uint32_t), st), "memset");
+  CU(cudaMemsetAsync(w.counters, 0, 16 * sizeof(uint32_t), st), "memset");
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
   if (nG > 0) {
@@ -337,9 +339,12 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
   }
   // The shared-memory tier runs in size bands, each launch sized for its own
   // largest pivot, so that the many small pivots are not held to the
-  // occupancy of the largest one.
-  static const uint32_t bands[] = {kCliqueSmemMax, 512, 256, 128, 32};
+  // occupancy of the largest one.  Band edges where the CTAs per SM change
+  // (1 above 1,024 entries, 3 up to 1,024, 5 up to 768, 6 -- the register
+  // limit -- up to 512); fewer bands mean fewer drained-GPU tails.
+  const uint32_t bands[] = {cap, 1024, 768, 512, 32};
   for (int b = 0; b + 1 < (int)(sizeof(bands) / sizeof(bands[0])); b++) {
+    if (bands[b] <= bands[b + 1]) continue;
     const uint32_t p0 = p.above(bands[b]), p1 = p.above(bands[b + 1]);
     if (p1 <= p0) continue;
     const uint32_t cmax = p.largest_at_most(bands[b]);
@@ -347,7 +352,7 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
   }
   if (nL > nB) {
     const int grid = (int)std::min<uint64_t>((nL - nB + 63) / 64, 8ull * sms);
-    CU(launch_clique_light(a, nB, nL, w.counters + 7, grid > 0 ? grid : 1, st), "clique kernel (warp)");
+    CU(launch_clique_light(a, nB, nL, w.counters + 11, grid > 0 ? grid : 1, st), "clique kernel (warp)");
   }
   return EH_OK;
 }

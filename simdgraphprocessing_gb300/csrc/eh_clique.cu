@@ -16,8 +16,10 @@
 //   k > 4: depth-first over the same masks.
 // Tiers by |A_i| (rows sorted by descending size): one warp per pivot with
 // one-word masks (|A_i| <= 32); one CTA per pivot with masks in shared memory
-// (|A_i| <= kCliqueSmemMax); one CTA per pivot with masks in a global scratch
-// slot (larger pivots).
+// (up to clique_smem_cap(k), about 1,650-1,850 entries), launched in size bands
+// so that each launch's shared memory (and so its CTAs per SM) fits its own
+// largest pivot; one CTA per pivot with masks in a global scratch slot (larger
+// pivots).  The masks are stored as a packed lower-triangular bit matrix.
 #include <algorithm>
 #include <atomic>
 #include <map>
@@ -33,6 +35,20 @@ namespace {
 constexpr int NW = kCtaThreads / 32;
 
 __device__ __forceinline__ uint32_t ilog2p1_c(uint32_t x) { return 32u - __clz(x | 1u); }
+
+// Packed lower-triangular masks: row e holds bits < e in mask_len(e) words
+// (ceil(e/32), made odd so that lanes reading rows e, e+1, ... at the same word
+// index fall in different shared-memory banks); mask_off(e) = sum of the
+// lengths of rows 0 .. e-1.  A c-entry pivot needs mask_off(c) words, about
+// half of a c x c bit matrix.
+__host__ __device__ __forceinline__ uint32_t mask_len(uint32_t e) { return ((e + 31) >> 5) | 1u; }
+// 32-bit arithmetic: exact for e < 65,536 (mask_off(65535) < 2^27).
+__host__ __device__ __forceinline__ uint32_t mask_off(uint32_t e) {
+  if (e == 0) return 0;
+  const uint32_t A = (e - 1) >> 5, r = (e - 1) & 31;
+  // row 0: 1 word; rows 32a+1 .. 32a+32: (a+1)|1 words each.
+  return 1 + 32 * (A * (A + 1) / 2 + A / 2) + r * ((A + 1) | 1);
+}
 
 // ---- light tier: |A_i| <= 32, one warp per pivot, one-word masks ----
 __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint32_t pos_begin,
@@ -125,9 +141,10 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
 }
 
 // ---- CTA tiers: one pivot per CTA; masks in shared memory or a global slot ----
-// Per CTA working set (words): list[cmax] | masks[cmax * W] | stacks[NW][2 * (k-2) * W]
+// Per CTA working set (words): list[cmax] | masks[mask_off(cmax)] | stacks[NW][2 * (k-2) * W]
+// (stacks only for k >= 5); W = mask_len(cmax) is the DFS stack row length.
 template <bool GLOBAL>
-__global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32_t pos_begin, uint32_t pos_end,
+__global__ void __launch_bounds__(kCtaThreads, GLOBAL ? 2 : 8) k_clique_cta(CliqueArgs a, uint32_t pos_begin, uint32_t pos_end,
                                                             uint32_t* counter, uint32_t cmax, uint32_t W,
                                                             uint32_t* gscratch, uint64_t slot_words) {
   extern __shared__ __align__(16) uint32_t dyn[];
@@ -138,7 +155,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
   uint32_t* list = base;
   uint32_t* masks = base + cmax;
   const uint32_t stack_words = 2u * (a.k - 2) * W;
-  uint32_t* stack = masks + (uint64_t)cmax * W + (uint64_t)warp * stack_words;
+  uint32_t* stack = masks + mask_off(cmax) + (uint64_t)warp * stack_words;
   const int top = (int)a.k - 3;
   unsigned long long acc = 0;
   for (;;) {
@@ -151,12 +168,12 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
     const uint32_t c = A.card;
     const unsigned long long acc_before = acc;
     cta_decode<kCtaThreads>(A, list, s_scan);
-    for (uint64_t x = threadIdx.x; x < (uint64_t)c * W; x += kCtaThreads) masks[x] = 0;
+    for (uint64_t x = threadIdx.x; x < mask_off(c); x += kCtaThreads) masks[x] = 0;
     __syncthreads();
     // phase 1: warp per e builds M[e]
     for (uint32_t e = 1 + warp; e < c; e += NW) {
       const uint32_t j = list[e];
-      uint32_t* Me = masks + (uint64_t)e * W;
+      uint32_t* Me = masks + mask_off(e);
       if (j < a.core_k) {  // core row j = row(j) ∩ [0, j): one word per probe, L2-resident
         const unsigned long long* row = a.core + core_row_offset(j);
         for (uint32_t b = 0; b < e; b += 32) {
@@ -189,12 +206,13 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
     __syncthreads();
     // phase 2: warp per e
     for (uint32_t e = 1 + warp; e < c; e += NW) {
-      const uint32_t* Me = masks + (uint64_t)e * W;
+      const uint32_t* Me = masks + mask_off(e);
       const uint32_t we = (e + 31) >> 5;  // words that can hold bits < e
       if (top == 0) {
         for (uint32_t w = lane; w < we; w += 32) acc += __popc(Me[w]);
       } else if (top == 1) {
-        // k = 4: sum over t in M[e] of popc(M[e] & M[t]); M[t] has no bits at or above t.
+        // k = 4: sum over t in M[e] of popc(M[e] & M[t]); M[t] has bits below t only,
+        // in its ceil(t/32) words.
         if (GLOBAL && we > 8) {
           // Long rows in global memory: the warp walks the set bits t together and
           // lanes take consecutive words of the two rows (coalesced reads).
@@ -203,19 +221,22 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
             while (bits) {
               const uint32_t t = 32 * w0 + (__ffs(bits) - 1);
               bits &= bits - 1;
-              const uint32_t* Mt = masks + (uint64_t)t * W;
-              for (uint32_t x = lane; x <= (t >> 5); x += 32) acc += __popc(Me[x] & Mt[x]);
+              const uint32_t* Mt = masks + mask_off(t);
+              for (uint32_t x = lane; x < ((t + 31) >> 5); x += 32) acc += __popc(Me[x] & Mt[x]);
             }
           }
         } else {
-          // Each lane takes one t of a word of M[e]; the odd row stride W keeps the
+          // Each lane takes one t of a word of M[e]; odd row lengths keep the
           // lanes' rows in different shared-memory banks.
           for (uint32_t w = 0; w < we; w++) {
             const uint32_t bits = Me[w];
             if (!((bits >> lane) & 1u)) continue;
             const uint32_t t = 32 * w + lane;
-            const uint32_t* Mt = masks + (uint64_t)t * W;
-            for (uint32_t x = 0; x <= (t >> 5); x++) acc += __popc(Me[x] & Mt[x]);
+            // mask_off(t) from the word's first row: rows 32w+1 .. 32w+31 are (w+1)|1
+            // words long, row 32w is w|1 words long.
+            const uint32_t first = mask_off(32 * w + 1);
+            const uint32_t* Mt = masks + (lane ? first + (lane - 1) * ((w + 1) | 1u) : first - (w | 1u));
+            for (uint32_t x = 0; x < ((t + 31) >> 5); x++) acc += __popc(Me[x] & Mt[x]);
           }
         }
       } else {
@@ -251,12 +272,13 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
           }
           __syncwarp();
           if (lane == 0) Rd[t >> 5] &= ~(1u << (t & 31));
-          const uint32_t* Mt = masks + (uint64_t)t * W;
+          const uint32_t* Mt = masks + mask_off(t);
+          const uint32_t lt = (t + 31) >> 5;  // words of M[t]; the rest are 0
           uint32_t* Sn = S + (uint64_t)(d + 1) * W;
           uint32_t* Rn = R + (uint64_t)(d + 1) * W;
           uint32_t cnt = 0;
           for (uint32_t w = lane; w < W; w += 32) {
-            const uint32_t v = Sd[w] & Mt[w];
+            const uint32_t v = w < lt ? Sd[w] & Mt[w] : 0u;
             Sn[w] = v;
             Rn[w] = v;
             cnt += __popc(v);
@@ -280,13 +302,27 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_cta(CliqueArgs a, uint32
 
 }  // namespace
 
-// Mask row stride in words: enough for cmax bits, odd so that lanes reading
-// different rows hit different shared-memory banks.
-static uint32_t mask_stride(uint32_t cmax) { return ((cmax + 31) / 32) | 1u; }
-
 uint64_t clique_slot_words(uint32_t cmax, uint32_t k) {
-  const uint64_t W = mask_stride(cmax);
-  return (uint64_t)cmax + (uint64_t)cmax * W + (uint64_t)NW * 2 * (k - 2) * W;
+  const uint64_t W = mask_len(cmax);
+  return (uint64_t)cmax + (uint64_t)mask_off(cmax) + (k >= 5 ? (uint64_t)NW * 2 * (k - 2) * W : 0);
+}
+
+uint32_t clique_smem_cap(uint32_t k, int device) {
+  static std::atomic<int> optin[64];
+  int o = (device >= 0 && device < 64) ? optin[device].load() : 0;
+  if (o <= 0) {
+    cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (device >= 0 && device < 64) optin[device].store(o);
+  }
+  // Leave room for the kernel's static shared memory (s_unit, s_scan).
+  const uint64_t budget = o > 2048 ? (uint64_t)o - 2048 : 0;
+  uint32_t lo = 32, hi = kCliqueSmemMax;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) / 2;
+    if (clique_slot_words(mid, k) * 4 <= budget) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
 // SMs x resident CTAs of the shared-memory clique kernel with `bytes` of
@@ -316,7 +352,7 @@ cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_
 cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                               uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st) {
   if (pos_end <= pos_begin) return cudaSuccess;
-  const uint32_t W = mask_stride(cmax);
+  const uint32_t W = mask_len(cmax);
   const uint64_t slot = clique_slot_words(cmax, a.k);
   if (gscratch) {
     k_clique_cta<true><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch, slot);

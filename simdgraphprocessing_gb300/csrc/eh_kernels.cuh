@@ -125,11 +125,14 @@ struct CliqueArgs {
   uint32_t core_k;
 };
 constexpr uint32_t kCliqueMaxK = 16;
-constexpr uint32_t kCliqueSmemMax = 1024;  // pivots up to this size keep their masks in shared memory
+constexpr uint32_t kCliqueSmemMax = 2048;  // no pivot above this size keeps its masks in shared memory
 // Words of one pivot's working set (list, masks, per-warp DFS stacks).
 uint64_t clique_slot_words(uint32_t cmax, uint32_t k);
 cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                                 int grid, cudaStream_t st);
+// Largest pivot (<= kCliqueSmemMax) whose k-clique working set fits one CTA's
+// opt-in shared memory on `device`; larger pivots use global scratch slots.
+uint32_t clique_smem_cap(uint32_t k, int device);
 // gscratch == nullptr: masks in dynamic shared memory (grid <= 0: as many CTAs
 // as fit on the GPU, at most one per pivot); else grid slots of
 // clique_slot_words(cmax, k) words each in global memory.

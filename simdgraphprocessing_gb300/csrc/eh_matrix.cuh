@@ -41,7 +41,7 @@ struct Plan {
 // A matrix has its own; concurrent launches on one matrix (the serving loop)
 // each bring theirs.
 struct Workspace {
-  uint32_t* counters = nullptr;        // >= 8 words
+  uint32_t* counters = nullptr;        // >= 16 words
   uint32_t* clique_scratch = nullptr;
   uint64_t clique_scratch_words = 0;
 };
@@ -55,7 +55,7 @@ struct Matrix {
   uint64_t arena_units = 0;
   BuildTotals tot{};
   Plan plan;
-  uint32_t* counters = nullptr;
+  uint32_t* counters = nullptr;  // 16 work-queue counters, then `result`
   unsigned long long* result = nullptr;
   int grid = 0;
   int64_t vstar = -1;

@@ -87,7 +87,8 @@ extern "C" eh_status eh_count_cliques_noalloc(eh_matrix_t mh, uint32_t k, uint64
   if (e != cudaSuccess) return set_error(EH_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
   if (k < 3) return EH_OK;  // as eh_count_cliques: the reference returns 0 for n < 3
   const Plan& p = m->plan;
-  const uint32_t nG = p.above(kCliqueSmemMax);
+  const uint32_t cap = clique_smem_cap(k, m->device);
+  const uint32_t nG = p.above(cap);
   const uint32_t nB = p.above(32);
   const uint32_t nL = p.above(k - 2);
   uint32_t* counters = scratch;
@@ -114,7 +115,7 @@ extern "C" eh_status eh_count_cliques_noalloc(eh_matrix_t mh, uint32_t k, uint64
     if (e != cudaSuccess) return set_error(EH_ERR_CUDA, "clique kernel (fixed scratch): %s", cudaGetErrorString(e));
   }
   if (nB > nG) {
-    const uint32_t cmax = p.largest_at_most(kCliqueSmemMax);
+    const uint32_t cmax = p.largest_at_most(cap);
     const int grid = (int)std::min<uint64_t>(nB - nG, 4ull * sms);
     e = launch_clique_cta(a, nG, nB, counters + 3, cmax, nullptr, grid, st);
     if (e != cudaSuccess) return set_error(EH_ERR_CUDA, "clique kernel (shared): %s", cudaGetErrorString(e));

@@ -86,7 +86,7 @@ namespace {
 uint64_t query_scratch_words(const GraphEntry& ge, uint32_t kind, uint32_t k, int sms) {
   if (kind != EH_QUERY_CLIQUES || k < 3) return 0;
   const Matrix* m = ge.low;
-  const uint32_t nG = m->plan.above(kCliqueSmemMax);
+  const uint32_t nG = m->plan.above(clique_smem_cap(k, m->device));
   if (!nG) return 0;
   const uint64_t grid = std::min<uint64_t>(nG, 2ull * sms);
   return clique_slot_words((uint32_t)m->tot.max_card, k) * grid;

@@ -172,17 +172,26 @@ def complete_graphs(sizes):
 @pytest.mark.parametrize("layout", LAYOUTS)
 def test_cliques_closed_form_all_tiers(eh, layout):
     from math import comb
-    sizes = [1100, 600, 200, 30, 5]  # global-scratch, shared-memory and warp tiers
+    # Pivots of K_1900 above ~1,850 entries do not fit shared memory and use the
+    # global-scratch tier; the rest of K_1900, K_1100 and K_600 cover the
+    # shared-memory size bands, K_30 and K_5 the warp tier.
+    sizes = [1900, 1100, 600, 200, 30, 5] if layout == "hybrid" else [1100, 600, 200, 30, 5]
     off, nbr = complete_graphs(sizes)
     g = eh.HostGraph.from_csr(off, nbr).reorder_by_degree()
     off, nbr = g.csr()[:2]
     m = eh.Matrix.build(off, nbr, selection="lower", layout=layout)
     assert m.info()["max_row_cardinality"] > 1024
-    # Work grows with the number of (k-1)-cliques: k <= 5 keeps K_1100 at ~2e8 search nodes
-    # (run for one layout; the masks, not the layout, carry the search).
-    for k in ((3, 4, 5) if layout == "hybrid" else (3, 4)):
+    for k in (3, 4):
         assert m.count_cliques(k) == sum(comb(s, k) for s in sizes), k
     assert m.count_triangles() == sum(comb(s, 3) for s in sizes)
+    # Work grows with the number of (k-1)-cliques: k = 5 on K_1100 is ~2e8 search
+    # nodes (run for one layout; the masks, not the layout, carry the search).
+    if layout == "hybrid":
+        sizes5 = [1100, 600, 200, 30, 5]
+        off5, nbr5 = complete_graphs(sizes5)
+        g5 = eh.HostGraph.from_csr(off5, nbr5).reorder_by_degree()
+        m5 = eh.Matrix.build(*g5.csr()[:2], selection="lower", layout=layout)
+        assert m5.count_cliques(5) == sum(comb(s, 5) for s in sizes5)
     # Deeper k on small cliques: the search visits every (k-1)-clique, so K_40 with
     # k <= 8 (about 2e7 nodes, shared-memory tier) and K_20 up to k = 16 (warp tier).
     for small, ks in (([40, 33], (6, 8)), ([20, 18, 12, 7], (12, 16))):

@@ -32,8 +32,8 @@ def complete_graphs(sizes, seed=9):
 
 
 def graphs(eh):
-    g = eh.HostGraph.from_csr(*complete_graphs([1100, 600, 200, 30])).reorder_by_degree()
-    yield "complete", g.csr()[:2]  # pivots above 1,024 entries use the fixed scratch slots
+    g = eh.HostGraph.from_csr(*complete_graphs([1900, 600, 200, 30])).reorder_by_degree()
+    yield "complete", g.csr()[:2]  # pivots above ~1,850 entries (too big for shared memory) use the fixed scratch
     yield "rmat", eh.graph("rmat", 12, scale=12, edges=40000).csr()[:2]
 
 
