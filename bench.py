@@ -43,6 +43,9 @@ def parse_args():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--scale", type=int, default=22)
     p.add_argument("--edge-factor", type=int, default=16)
+    p.add_argument("--edges", type=int, default=0,
+                   help="exact undirected edge count (overrides the edge factor; e.g. the uint workload: "
+                        "--scale 16 --edges 1000000 --seed 1 --layout uint)")
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--layout", default="hybrid")
     p.add_argument("--e2e-steps", type=int, default=3)
@@ -61,11 +64,16 @@ def parse_args():
     return p.parse_args()
 
 
+def edge_count(a):
+    return a.edges if a.edges else a.edge_factor << a.scale
+
+
 def workload(a):
+    size = ("%d edges" % a.edges) if a.edges else ("edge factor %d" % a.edge_factor)
     return {
-        "workload": "undirected triangle count, R-MAT scale %d edge factor %d (a=.57,b=.19,c=.19), "
-                    "seed %d, %s layout, degree-ordered, nbr<node pruning" % (a.scale, a.edge_factor, a.seed, a.layout),
-        "graph": "rmat", "scale": a.scale, "undirected_edges": a.edge_factor << a.scale, "seed": a.seed,
+        "workload": "undirected triangle count, R-MAT scale %d %s (a=.57,b=.19,c=.19), "
+                    "seed %d, %s layout, degree-ordered, nbr<node pruning" % (a.scale, size, a.seed, a.layout),
+        "graph": "rmat", "scale": a.scale, "undirected_edges": edge_count(a), "seed": a.seed,
         "layout": a.layout,
     }
 
@@ -151,7 +159,7 @@ def aggregate(units_per_rank, ms_per_rank, world, device=None):
 
 def make_graph(a):
     import simdgraphprocessing_gb300 as eh
-    g = eh.graph("rmat", a.seed, scale=a.scale, edges=a.edge_factor << a.scale)
+    g = eh.graph("rmat", a.seed, scale=a.scale, edges=edge_count(a))
     off, nbr, _, _ = g.csr()
     return off, nbr
 

@@ -51,28 +51,69 @@ __device__ __forceinline__ bool sym_heavy(const RowView& A, const RowView& B) {
   return min(A.card, B.card) > kSymLight;
 }
 
+constexpr uint32_t kSymChunk = 32;  // rows a warp takes per grab (one per lane)
+constexpr uint32_t kSymTiny = 64;   // uint rows a single lane intersects by merging
+
 __device__ __forceinline__ bool sym_above(uint32_t both, const RowView& A, const RowView& B, double threshold) {
   // 0 / 0 is NaN, which is not above any threshold (as in the reference).
   return (double)both / (double)((uint64_t)A.card + B.card - both) > threshold;
 }
 
-__global__ void __launch_bounds__(256) k_symbiosity(uint64_t n, const RowDesc* __restrict__ dr,
+// |A ∩ B| of two sorted uint rows by one thread (a merge).
+__device__ __forceinline__ uint32_t merge_count(const uint32_t* a, uint32_t na, const uint32_t* b, uint32_t nb) {
+  uint32_t i = 0, j = 0, c = 0;
+  while (i < na && j < nb) {
+    const uint32_t x = a[i], y = b[j];
+    c += x == y;
+    i += x <= y;
+    j += y <= x;
+  }
+  return c;
+}
+
+// Rows are taken kSymChunk at a time from a shared cursor, one row per lane.
+// A lane finishes its row alone when both sides are uint rows of at most
+// kSymTiny entries (most rows of a sparse graph) or one side is empty; rows
+// above that go to the whole warp, and rows too long for a warp to the list
+// of k_symbiosity_heavy.
+__global__ void __launch_bounds__(256, 6) k_symbiosity(uint32_t n, const RowDesc* __restrict__ dr,
                                                     const uint4* __restrict__ ar, const RowDesc* __restrict__ dc,
                                                     const uint4* __restrict__ ac, double threshold,
-                                                    unsigned long long* out, uint32_t* heavy, uint32_t* n_heavy) {
+                                                    unsigned long long* out, uint32_t* heavy, uint32_t* n_heavy,
+                                                    uint32_t* cursor) {
   const uint32_t lane = threadIdx.x & 31;
   unsigned long long acc = 0;
-  const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
-  for (uint64_t r = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < n; r += nw) {
-    const RowView A = load_view(dr, ar, (uint32_t)r);
-    const RowView B = load_view(dc, ac, (uint32_t)r);
-    if (sym_heavy(A, B)) {
-      if (lane == 0) heavy[atomicAdd(n_heavy, 1u)] = (uint32_t)r;
-      continue;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(cursor, kSymChunk);
+    base = __shfl_sync(FULL, base, 0);
+    if (base >= n) break;
+    const uint32_t r = base + lane;
+    bool warp_row = false;
+    if (r < n) {
+      const RowView A = load_view(dr, ar, r);
+      const RowView B = load_view(dc, ac, r);
+      if (!A.card || !B.card) {  // ratio 0, or 0/0 (NaN, never above)
+        acc += sym_above(0, A, B, threshold);
+      } else if (A.type == TY_UINT && B.type == TY_UINT && max(A.card, B.card) <= kSymTiny) {
+        const uint32_t both = merge_count(static_cast<const uint32_t*>(A.p), A.card,
+                                          static_cast<const uint32_t*>(B.p), B.card);
+        acc += sym_above(both, A, B, threshold);
+      } else if (sym_heavy(A, B)) {
+        heavy[atomicAdd(n_heavy, 1u)] = r;
+      } else {
+        warp_row = true;
+      }
     }
-    const uint32_t both = warp_intersect_size(A, B, lane);
-    if (lane == 0 && sym_above(both, A, B, threshold)) acc++;
+    for (uint32_t wm = __ballot_sync(FULL, warp_row); wm; wm &= wm - 1) {
+      const uint32_t r2 = base + (__ffs(wm) - 1);
+      const RowView A = load_view(dr, ar, r2);
+      const RowView B = load_view(dc, ac, r2);
+      const uint32_t both = warp_intersect_size(A, B, lane);
+      if (lane == 0) acc += sym_above(both, A, B, threshold);
+    }
   }
+  acc = warp_sum_u64(acc);
   if (lane == 0 && acc) atomicAdd(out, acc);
 }
 
@@ -320,20 +361,21 @@ extern "C" eh_status eh_symbiosity_async(eh_matrix_t rh, eh_matrix_t ch, double 
   cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(uint64_t), st);
   if (e != cudaSuccess) return cuda_err(e, "memset");
   if (r->n == 0) return EH_OK;
-  // Heavy-row list: n entries, then its length and the CTAs' cursor.
+  // Heavy-row list: n entries, then its length, the CTAs' cursor and the warps' cursor.
   uint32_t* scratch = nullptr;
-  e = cudaMallocAsync((void**)&scratch, (r->n + 2) * sizeof(uint32_t), st);
+  e = cudaMallocAsync((void**)&scratch, (r->n + 3) * sizeof(uint32_t), st);
   if (e != cudaSuccess) return set_error(EH_ERR_OUT_OF_MEMORY, "symbiosity scratch: %s", cudaGetErrorString(e));
   uint32_t* counts = scratch + r->n;
-  e = cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st);
+  e = cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st);
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, r->device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_symbiosity_heavy, 256, 0);
   if (e == cudaSuccess) {
-    const uint64_t g = std::min<uint64_t>((r->n + 7) / 8, 152ull * 32);
+    const uint64_t g = std::min<uint64_t>((r->n + 8 * kSymChunk - 1) / (8 * kSymChunk), (uint64_t)sms * 8);
     unsigned long long* out = reinterpret_cast<unsigned long long*>(d_count);
-    k_symbiosity<<<(unsigned)g, 256, 0, st>>>(r->n, r->desc, r->arena, c->desc, c->arena, threshold, out, scratch,
-                                              counts);
+    k_symbiosity<<<(unsigned)std::max<uint64_t>(g, 1), 256, 0, st>>>((uint32_t)r->n, r->desc, r->arena, c->desc,
+                                                                     c->arena, threshold, out, scratch, counts,
+                                                                     counts + 2);
     k_symbiosity_heavy<<<(unsigned)(sms * std::max(per, 1)), 256, 0, st>>>(r->desc, r->arena, c->desc, c->arena,
                                                                            threshold, out, scratch, counts,
                                                                            counts + 1);

@@ -68,7 +68,7 @@ def test_symbiosity_vs_oracle(eh, oracle, name, layout):
     a = arrays_of(eh, name)
     rows, cols = _pair(eh, a, layout)
     orows, ocols = _opair(oracle, a, layout)
-    for thr in (0.5, 0.0, 0.25, 0.9):
+    for thr in (0.5, 0.0, 0.25, 0.9, -1.0):
         assert rows.symbiosity(cols, thr) == orows.symbiosity(ocols, thr), thr
     # Undirected use: the rows are their own columns.
     assert rows.symbiosity() == orows.symbiosity()
