@@ -3,11 +3,13 @@
 // pack_data (:249-266), the layout optimizer hybrid::get_type
 // (src/set/layouts/hybrid.hpp:73-100) and the encoders T::build_flattened.
 //
-// Pass 1 (k_measure, one warp per row): validate the row (strictly ascending,
-// ids < n), apply the edge selection, and measure what the layout needs
+// Pass 1 (k_measure, one warp per row): validate the row (offsets rising within
+// the neighbour array, strictly ascending, ids < n), apply the edge selection,
+// and measure what the layout needs
 // (count, first, last, 16-bit partitions).  Choose the layout and payload size.
 // Pass 2: exclusive scan of payload sizes (16-byte units) -> row offsets.
 // Pass 3 (k_encode, one warp per row): write RowDesc and the payload.
+#include <algorithm>
 #include <cstdint>
 
 #include "eh_kernels.cuh"
@@ -24,122 +26,247 @@ __device__ __forceinline__ bool is_selected(int sel, uint32_t x, uint64_t row, c
   return mask[k] != 0;
 }
 
-__global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, const uint64_t* __restrict__ off,
+// Rows longer than this are measured and encoded by a whole CTA (k_*_big): a
+// hub row of a degree-ordered graph would otherwise keep one warp busy long
+// after the rest of the grid has finished.
+constexpr uint64_t kBigRow = 4096;
+constexpr int kBigBlock = 1024;
+
+struct SegMeasure {
+  uint32_t cnt, parts, first, last, first_hi, last_hi, flags;
+};
+
+// One warp measures elements [s0, s1) of `row`: selected count, 16-bit
+// partitions (the segment's first selected element counts as a new one),
+// first / last selected, and validation flags.  `before` is the element at
+// s0 - 1 when s0 > row_begin (for the strictly-ascending check).
+__device__ __forceinline__ SegMeasure measure_segment(uint64_t n, uint64_t row, uint64_t row_begin, uint64_t s0,
+                                                      uint64_t s1, uint32_t before,
+                                                      const uint32_t* __restrict__ nbr,
+                                                      const uint8_t* __restrict__ mask, int sel, uint32_t lane) {
+  SegMeasure r{0, 0, 0xffffffffu, 0, 0, 0, 0};
+  uint32_t carry = 0, last_sel = 0;
+  bool have_carry = false;
+  for (uint64_t base = s0; base < s1; base += 32) {
+    const uint64_t k = base + lane;
+    const bool valid = k < s1;
+    const uint32_t x = valid ? nbr[k] : 0u;
+    // The element before x: from the lane below, or the previous round's last.
+    const uint32_t up = __shfl_up_sync(FULL, x, 1);
+    const uint32_t prev_raw = lane ? up : before;
+    before = __shfl_sync(FULL, x, 31);
+    if (valid) {
+      if (x >= n) r.flags |= ERRF_RANGE;
+      if (k > row_begin && prev_raw >= x) r.flags |= ERRF_UNSORTED;
+    }
+    const bool s = valid && is_selected(sel, x, row, mask, k);
+    const uint32_t bal = __ballot_sync(FULL, s);
+    if (s) {
+      r.first = min(r.first, x);
+      r.last = max(r.last, x);
+    }
+    // Previous selected element (for counting distinct 16-bit prefixes).
+    const uint32_t lower = bal & ((1u << lane) - 1u);
+    const int src = lower ? 31 - __clz(lower) : (int)lane;
+    const uint32_t px = __shfl_sync(FULL, x, src);
+    const bool has_prev = lower != 0 || have_carry;
+    const uint32_t prev = lower ? px : carry;
+    const bool new_part = s && (!has_prev || (prev >> 16) != (x >> 16));
+    r.parts += __popc(__ballot_sync(FULL, new_part));
+    if (bal) {
+      carry = __shfl_sync(FULL, x, 31 - __clz(bal));
+      have_carry = true;
+      last_sel = carry;
+    }
+    r.cnt += __popc(bal);
+  }
+  r.first = __reduce_min_sync(FULL, r.first);
+  r.last = __reduce_max_sync(FULL, r.last);
+  r.first_hi = r.first >> 16;
+  r.last_hi = last_sel >> 16;
+  r.flags = __reduce_or_sync(FULL, r.flags);
+  return r;
+}
+
+struct RowResult {
+  RowMeasure m;
+  uint64_t ref;
+  uint32_t type;
+};
+
+// Layout choice and payload size of one row from its measure (hybrid::get_type,
+// src/set/layouts/hybrid.hpp:73-100; the three-tier rule for layout 16).
+__device__ __forceinline__ RowResult finish_row(uint32_t cnt, uint32_t parts, uint32_t first, uint32_t last,
+                                                int layout) {
+  uint32_t type;
+  if (layout == TY_UINT) type = TY_UINT;
+  else if (layout == TY_BITSET) type = TY_BITSET;
+  else if (layout == TY_PSHORT) type = TY_PSHORT;
+  else {
+    type = TY_UINT;
+    if (cnt > 1 && last > first) {
+      // The reference tests the double quotient cnt / range against 1/256 (and
+      // 1/32).  With integers below 2^53 that equals the integer test
+      // 256 * cnt > range: if 256 * cnt > range the quotient exceeds 2^-8 by at
+      // least 1 / (256 * range) > 2^-61, more than half an ulp of 2^-8, so the
+      // rounded quotient is still above it; otherwise it is at most 2^-8.
+      const uint64_t range = (uint64_t)(last - first);
+      if (layout == 16) {  // three-tier rule (hybrid::compute_type)
+        if (32ull * cnt > range) type = TY_BITSET;
+        else if (256ull * cnt > range) type = TY_PSHORT;
+      } else if (256ull * cnt > range) {  // hybrid::get_type
+        type = TY_BITSET;
+      }
+    }
+  }
+  uint32_t len = 0, aux = 0;
+  uint64_t bytes = 0, ref = 0;
+  if (type == TY_UINT) {
+    len = cnt;
+    bytes = 4ull * cnt;
+    ref = bytes;
+  } else if (type == TY_BITSET) {
+    if (cnt) {
+      aux = first >> 6;
+      len = (last >> 6) - aux + 1;
+      ref = 4 + 8 + 8ull * len;
+    }
+    bytes = 8ull * len;
+  } else {
+    if (cnt) {
+      aux = parts;
+      len = cnt + 2 * parts;
+      ref = 4 + 2ull * len;
+    }
+    bytes = 2ull * len;
+  }
+  const bool hybrid = (layout != TY_UINT && layout != TY_BITSET && layout != TY_PSHORT);
+  if (hybrid) ref += 8;
+  const uint32_t units = (uint32_t)((bytes + 15) / 16);
+  return RowResult{RowMeasure{cnt, aux, make_lt(type, len), units}, ref, type};
+}
+
+struct Totals {
+  unsigned long long card = 0, ref = 0, units = 0, max_full = 0, max_card = 0;
+  uint32_t n_uint = 0, n_pshort = 0, n_bitset = 0;
+  __device__ __forceinline__ void add(const RowResult& r, uint64_t full) {
+    card += r.m.card;
+    ref += r.ref;
+    units += r.m.units;
+    n_uint += r.type == TY_UINT;
+    n_pshort += r.m.card && r.type == TY_PSHORT;
+    n_bitset += r.m.card && r.type == TY_BITSET;
+    max_full = max(max_full, (unsigned long long)full);
+    max_card = max(max_card, (unsigned long long)r.m.card);
+  }
+  __device__ __forceinline__ void flush(BuildTotals* tot) const {
+    if (card) atomicAdd(&tot->cardinality, card);
+    if (ref) atomicAdd(&tot->ref_bytes, ref);
+    if (n_uint) atomicAdd(&tot->num_uint, (unsigned long long)n_uint);
+    if (n_pshort) atomicAdd(&tot->num_pshort, (unsigned long long)n_pshort);
+    if (n_bitset) atomicAdd(&tot->num_bitset, (unsigned long long)n_bitset);
+    if (units) atomicAdd(&tot->payload_units, units);
+    if (max_full) atomicMax(&tot->max_full_degree, max_full);
+    if (max_card) atomicMax(&tot->max_card, max_card);
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, uint64_t total, const uint64_t* __restrict__ off,
                                                     const uint32_t* __restrict__ nbr,
                                                     const uint8_t* __restrict__ mask, int sel,
                                                     int layout, RowMeasure* __restrict__ meas,
                                                     BuildTotals* __restrict__ tot,
-                                                    uint32_t* __restrict__ err) {
-  __shared__ unsigned long long s_sum[6];  // cardinality, ref_bytes, uint, pshort, bitset, units
-  __shared__ unsigned long long s_max[2];  // full degree, card
-  __shared__ uint32_t s_err;
-  if (threadIdx.x < 6) s_sum[threadIdx.x] = 0;
-  if (threadIdx.x < 2) s_max[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_err = 0;
-  __syncthreads();
+                                                    uint32_t* __restrict__ err, uint32_t* __restrict__ big,
+                                                    uint32_t* __restrict__ n_big) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
   uint32_t flags = 0;
-  for (uint64_t row = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row < n; row += nw) {
-    const uint64_t b = off[row], e = off[row + 1];
-    uint32_t cnt = 0, parts = 0, first = 0xffffffffu, last = 0, carry = 0;
-    bool have_carry = false;
-    for (uint64_t base = b; base < e; base += 32) {
-      const uint64_t k = base + lane;
-      const bool valid = k < e;
-      const uint32_t x = valid ? nbr[k] : 0u;
-      if (valid) {
-        if (x >= n) flags |= ERRF_RANGE;
-        if (k > b && nbr[k - 1] >= x) flags |= ERRF_UNSORTED;
+  Totals t;  // lane 0's running totals for this warp's rows (one atomic each at the end)
+  // Rows are dealt to warps round-robin (row = warp + i * warps, so that the
+  // degree-ordered hubs at the front spread over the grid); a warp loads the
+  // offsets of its next 32 rows at once (lane q: its q-th row), then measures
+  // them one by one.
+  for (uint64_t row0 = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row0 < n; row0 += nw * 32) {
+    const uint64_t my = row0 + lane * nw;
+    const uint64_t my_b = my < n ? off[my] : 0, my_e = my < n ? off[my + 1] : 0;
+    for (uint32_t q = 0; q < 32; q++) {
+      const uint64_t row = row0 + q * nw;
+      if (row >= n) break;
+      uint64_t b = __shfl_sync(FULL, my_b, q), e = __shfl_sync(FULL, my_e, q);
+      if (e < b || e > total) {  // offsets must rise monotonically within the nbr array
+        flags |= ERRF_OFFSETS;
+        b = e = 0;
       }
-      const bool s = valid && is_selected(sel, x, row, mask, k);
-      const uint32_t bal = __ballot_sync(FULL, s);
-      if (s) {
-        first = min(first, x);
-        last = max(last, x);
+      if (e - b > kBigRow) {
+        if (lane == 0) big[atomicAdd(n_big, 1u)] = (uint32_t)row;
+        continue;
       }
-      // Previous selected element (for counting distinct 16-bit prefixes).
-      const uint32_t lower = bal & ((1u << lane) - 1u);
-      const int src = lower ? 31 - __clz(lower) : (int)lane;
-      const uint32_t px = __shfl_sync(FULL, x, src);
-      const bool has_prev = lower != 0 || have_carry;
-      const uint32_t prev = lower ? px : carry;
-      const bool new_part = s && (!has_prev || (prev >> 16) != (x >> 16));
-      parts += __popc(__ballot_sync(FULL, new_part));
-      if (bal) {
-        carry = __shfl_sync(FULL, x, 31 - __clz(bal));
-        have_carry = true;
+      const SegMeasure sm = measure_segment(n, row, b, b, e, 0u, nbr, mask, sel, lane);
+      flags |= sm.flags;
+      if (lane == 0) {
+        const RowResult r = finish_row(sm.cnt, sm.parts, sm.first, sm.last, layout);
+        if (sm.cnt >= (1u << 28)) flags |= ERRF_ROW_TOO_LONG;
+        meas[row] = r.m;
+        t.add(r, e - b);
       }
-      cnt += __popc(bal);
-    }
-    first = __reduce_min_sync(FULL, first);
-    last = __reduce_max_sync(FULL, last);
-    if (lane == 0) {
-      uint32_t type;
-      if (layout == TY_UINT) type = TY_UINT;
-      else if (layout == TY_BITSET) type = TY_BITSET;
-      else if (layout == TY_PSHORT) type = TY_PSHORT;
-      else {
-        type = TY_UINT;
-        if (cnt > 1 && last > first) {
-          const double density = (double)cnt / (double)(last - first);
-          if (layout == 16) {  // three-tier rule (hybrid::compute_type)
-            if (density > 1.0 / 32.0) type = TY_BITSET;
-            else if (density > 1.0 / 256.0) type = TY_PSHORT;
-          } else if (density > 1.0 / 256.0) {  // hybrid::get_type
-            type = TY_BITSET;
-          }
-        }
-      }
-      uint32_t len = 0, aux = 0;
-      uint64_t bytes = 0, ref = 0;
-      if (cnt >= (1u << 28)) flags |= ERRF_ROW_TOO_LONG;
-      if (type == TY_UINT) {
-        len = cnt;
-        bytes = 4ull * cnt;
-        ref = bytes;
-      } else if (type == TY_BITSET) {
-        if (cnt) {
-          aux = first >> 6;
-          len = (last >> 6) - aux + 1;
-          ref = 4 + 8 + 8ull * len;
-        }
-        bytes = 8ull * len;
-      } else {
-        if (cnt) {
-          aux = parts;
-          len = cnt + 2 * parts;
-          ref = 4 + 2ull * len;
-        }
-        bytes = 2ull * len;
-      }
-      const bool hybrid = (layout != TY_UINT && layout != TY_BITSET && layout != TY_PSHORT);
-      if (hybrid) ref += 8;
-      const uint32_t units = (uint32_t)((bytes + 15) / 16);
-      meas[row] = RowMeasure{cnt, aux, make_lt(type, len), units};
-      atomicAdd(&s_sum[0], (unsigned long long)cnt);
-      atomicAdd(&s_sum[1], (unsigned long long)ref);
-      if (type == TY_UINT) atomicAdd(&s_sum[2], 1ull);
-      else if (cnt && type == TY_PSHORT) atomicAdd(&s_sum[3], 1ull);
-      else if (cnt && type == TY_BITSET) atomicAdd(&s_sum[4], 1ull);
-      atomicAdd(&s_sum[5], (unsigned long long)units);
-      atomicMax(&s_max[0], (unsigned long long)(e - b));
-      atomicMax(&s_max[1], (unsigned long long)cnt);
     }
   }
-  flags = __reduce_or_sync(FULL, flags);
-  if (lane == 0 && flags) atomicOr(&s_err, flags);
-  __syncthreads();
+  if (lane == 0) {
+    t.flush(tot);
+    if (flags) atomicOr(err, flags);
+  }
+}
+
+// Rows longer than kBigRow, one CTA of kBigBlock threads each: warp w measures
+// the w-th slice of the row; thread 0 merges the slices in order (a slice whose
+// first 16-bit partition continues the previous non-empty slice's last one does
+// not start a new partition).
+__global__ void __launch_bounds__(kBigBlock) k_measure_big(uint64_t n, const uint64_t* __restrict__ off,
+                                                           const uint32_t* __restrict__ nbr,
+                                                           const uint8_t* __restrict__ mask, int sel, int layout,
+                                                           RowMeasure* __restrict__ meas,
+                                                           BuildTotals* __restrict__ tot, uint32_t* __restrict__ err,
+                                                           const uint32_t* __restrict__ big,
+                                                           const uint32_t* __restrict__ n_big) {
+  constexpr int NWB = kBigBlock / 32;
+  __shared__ SegMeasure s_seg[NWB];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nb = *n_big;
+  Totals t;
+  uint32_t flags = 0;
+  for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
+    const uint64_t row = big[i];
+    const uint64_t b = off[row], e = off[row + 1];
+    const uint64_t slice = ((e - b + NWB - 1) / NWB + 31) & ~31ull;
+    const uint64_t s0 = min(e, b + warp * slice), s1 = min(e, s0 + slice);
+    const uint32_t before = s0 > b ? nbr[s0 - 1] : 0u;
+    const SegMeasure sm = measure_segment(n, row, b, s0, s1, before, nbr, mask, sel, lane);
+    if (lane == 0) s_seg[warp] = sm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t cnt = 0, parts = 0, first = 0xffffffffu, last = 0, prev_hi = 0;
+      bool any = false;
+      for (int w = 0; w < NWB; w++) {
+        const SegMeasure& g = s_seg[w];
+        flags |= g.flags;
+        if (!g.cnt) continue;
+        cnt += g.cnt;
+        parts += g.parts - (any && prev_hi == g.first_hi ? 1u : 0u);
+        first = min(first, g.first);
+        last = max(last, g.last);
+        prev_hi = g.last_hi;
+        any = true;
+      }
+      const RowResult r = finish_row(cnt, parts, first, last, layout);
+      if (cnt >= (1u << 28)) flags |= ERRF_ROW_TOO_LONG;
+      meas[row] = r.m;
+      t.add(r, e - b);
+    }
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    atomicAdd(&tot->cardinality, s_sum[0]);
-    atomicAdd(&tot->ref_bytes, s_sum[1]);
-    atomicAdd(&tot->num_uint, s_sum[2]);
-    atomicAdd(&tot->num_pshort, s_sum[3]);
-    atomicAdd(&tot->num_bitset, s_sum[4]);
-    atomicAdd(&tot->payload_units, s_sum[5]);
-    atomicMax(&tot->max_full_degree, s_max[0]);
-    atomicMax(&tot->max_card, s_max[1]);
-    if (s_err) atomicOr(err, s_err);
+    t.flush(tot);
+    if (flags) atomicOr(err, flags);
   }
 }
 
@@ -240,6 +367,33 @@ cudaError_t exclusive_scan(In in, uint64_t n, uint32_t* out, uint32_t* tmp, cuda
   return cudaGetLastError();
 }
 
+// Sequential partition writer (pshort::build, pshort.hpp:46-78): [hi][count-1][lo...].
+__device__ void write_pshort(uint16_t* s, uint64_t row, uint64_t b, uint64_t e, const uint32_t* __restrict__ nbr,
+                             const uint8_t* __restrict__ mask, int sel) {
+  uint32_t w = 0, size_pos = 1, plen = 0, high = 0;
+  bool started = false;
+  for (uint64_t k = b; k < e; k++) {
+    const uint32_t x = nbr[k];
+    if (!is_selected(sel, x, row, mask, k)) continue;
+    const uint32_t hi = x >> 16, lo = x & 0xffffu;
+    if (started && hi == high) {
+      plen++;
+      s[w++] = (uint16_t)lo;
+    } else {
+      if (started) s[size_pos] = (uint16_t)plen;
+      s[w] = (uint16_t)hi;
+      s[w + 1] = 0;
+      s[w + 2] = (uint16_t)lo;
+      size_pos = w + 1;
+      w += 3;
+      plen = 0;
+      high = hi;
+      started = true;
+    }
+  }
+  s[size_pos] = (uint16_t)plen;
+}
+
 __global__ void __launch_bounds__(kBlock) k_encode(uint64_t n, const uint64_t* __restrict__ off,
                                                    const uint32_t* __restrict__ nbr,
                                                    const uint8_t* __restrict__ mask, int sel,
@@ -248,74 +402,145 @@ __global__ void __launch_bounds__(kBlock) k_encode(uint64_t n, const uint64_t* _
                                                    RowDesc* __restrict__ desc, uint4* __restrict__ arena) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
-  for (uint64_t row = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row < n; row += nw) {
-    const RowMeasure m = meas[row];
-    const uint32_t type = m.lt >> 30;
-    if (lane == 0) desc[row] = RowDesc{off16[row], m.card, m.aux, m.lt};
-    if (m.card == 0) continue;
-    const uint64_t b = off[row], e = off[row + 1];
-    uint4* dst = arena + off16[row];
-    if (type == TY_PSHORT) {
-      // Sequential partition writer (pshort::build, pshort.hpp:46-78): [hi][count-1][lo...].
-      if (lane == 0) {
-        uint16_t* s = reinterpret_cast<uint16_t*>(dst);
-        uint32_t w = 0, size_pos = 1, plen = 0, high = 0;
-        bool started = false;
-        for (uint64_t k = b; k < e; k++) {
-          const uint32_t x = nbr[k];
-          if (!is_selected(sel, x, row, mask, k)) continue;
-          const uint32_t hi = x >> 16, lo = x & 0xffffu;
-          if (started && hi == high) {
-            plen++;
-            s[w++] = (uint16_t)lo;
+  // Rows are dealt to warps round-robin as in k_measure; lane q loads the measure,
+  // offsets and payload start of the warp's q-th next row and writes its
+  // RowDesc, then the warp writes the payloads one row after another (rows
+  // longer than kBigRow are left to k_encode_big).
+  for (uint64_t row0 = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row0 < n; row0 += nw * 32) {
+    const uint64_t my = row0 + lane * nw;
+    RowMeasure mm{0, 0, 0, 0};
+    uint64_t my_b = 0, my_e = 0;
+    uint32_t my_o = 0;
+    if (my < n) {
+      mm = meas[my];
+      my_o = off16[my];
+      my_b = off[my];
+      my_e = off[my + 1];
+      desc[my] = RowDesc{my_o, mm.card, mm.aux, mm.lt};
+    }
+    for (uint32_t q = 0; q < 32; q++) {
+      const uint64_t row = row0 + q * nw;
+      if (row >= n) break;
+      const uint32_t card = __shfl_sync(FULL, mm.card, q);
+      const uint32_t aux = __shfl_sync(FULL, mm.aux, q);
+      const uint32_t type = __shfl_sync(FULL, mm.lt, q) >> 30;
+      const uint64_t b = __shfl_sync(FULL, my_b, q), e = __shfl_sync(FULL, my_e, q);
+      if (card == 0 || e - b > kBigRow) continue;
+      uint4* dst = arena + __shfl_sync(FULL, my_o, q);
+      if (type == TY_PSHORT) {
+        if (lane == 0) write_pshort(reinterpret_cast<uint16_t*>(dst), row, b, e, nbr, mask, sel);
+        continue;
+      }
+      uint32_t k_sel = 0;
+      for (uint64_t base = b; base < e; base += 32) {
+        const uint64_t k = base + lane;
+        const bool valid = k < e;
+        const uint32_t x = valid ? nbr[k] : 0u;
+        const bool s = valid && is_selected(sel, x, row, mask, k);
+        const uint32_t bal = __ballot_sync(FULL, s);
+        if (s) {
+          if (type == TY_UINT) {
+            reinterpret_cast<uint32_t*>(dst)[k_sel + __popc(bal & ((1u << lane) - 1u))] = x;
           } else {
-            if (started) s[size_pos] = (uint16_t)plen;
-            s[w] = (uint16_t)hi;
-            s[w + 1] = 0;
-            s[w + 2] = (uint16_t)lo;
-            size_pos = w + 1;
-            w += 3;
-            plen = 0;
-            high = hi;
-            started = true;
+            unsigned long long* words = reinterpret_cast<unsigned long long*>(dst);
+            atomicOr(&words[(x >> 6) - aux], 1ull << (x & 63));
           }
         }
-        s[size_pos] = (uint16_t)plen;
+        k_sel += __popc(bal);
       }
-      continue;
-    }
-    uint32_t k_sel = 0;
-    for (uint64_t base = b; base < e; base += 32) {
-      const uint64_t k = base + lane;
-      const bool valid = k < e;
-      const uint32_t x = valid ? nbr[k] : 0u;
-      const bool s = valid && is_selected(sel, x, row, mask, k);
-      const uint32_t bal = __ballot_sync(FULL, s);
-      if (s) {
-        if (type == TY_UINT) {
-          reinterpret_cast<uint32_t*>(dst)[k_sel + __popc(bal & ((1u << lane) - 1u))] = x;
-        } else {
-          unsigned long long* words = reinterpret_cast<unsigned long long*>(dst);
-          atomicOr(&words[(x >> 6) - m.aux], 1ull << (x & 63));
-        }
-      }
-      k_sel += __popc(bal);
     }
   }
 }
 
+// Payloads of the rows longer than kBigRow, one CTA each: warp w writes the
+// w-th slice of the row (uint rows: at the slice's output position, from a
+// count pass over the slices; bitset rows: one atomic OR per element; pshort
+// rows keep the sequential writer).
+__global__ void __launch_bounds__(kBigBlock) k_encode_big(const uint64_t* __restrict__ off,
+                                                          const uint32_t* __restrict__ nbr,
+                                                          const uint8_t* __restrict__ mask, int sel,
+                                                          const RowMeasure* __restrict__ meas,
+                                                          const uint32_t* __restrict__ off16,
+                                                          uint4* __restrict__ arena, const uint32_t* __restrict__ big,
+                                                          const uint32_t* __restrict__ n_big) {
+  constexpr int NWB = kBigBlock / 32;
+  __shared__ uint32_t s_cnt[NWB];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nb = *n_big;
+  for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
+    const uint64_t row = big[i];
+    const RowMeasure m = meas[row];
+    const uint32_t type = m.lt >> 30;
+    if (m.card == 0) continue;
+    const uint64_t b = off[row], e = off[row + 1];
+    uint4* dst = arena + off16[row];
+    if (type == TY_PSHORT) {
+      if (threadIdx.x == 0) write_pshort(reinterpret_cast<uint16_t*>(dst), row, b, e, nbr, mask, sel);
+      continue;
+    }
+    const uint64_t slice = ((e - b + NWB - 1) / NWB + 31) & ~31ull;
+    const uint64_t s0 = min(e, b + warp * slice), s1 = min(e, s0 + slice);
+    if (type == TY_BITSET) {
+      unsigned long long* words = reinterpret_cast<unsigned long long*>(dst);
+      for (uint64_t k = s0 + lane; k < s1; k += 32) {
+        const uint32_t x = nbr[k];
+        if (is_selected(sel, x, row, mask, k)) atomicOr(&words[(x >> 6) - m.aux], 1ull << (x & 63));
+      }
+      continue;
+    }
+    uint32_t c = 0;
+    for (uint64_t base = s0; base < s1; base += 32) {
+      const uint64_t k = base + lane;
+      c += __popc(__ballot_sync(FULL, k < s1 && is_selected(sel, nbr[k < s1 ? k : s0], row, mask, k)));
+    }
+    if (lane == 0) s_cnt[warp] = c;
+    __syncthreads();
+    uint32_t k_sel = 0;
+    for (uint32_t w = 0; w < warp; w++) k_sel += s_cnt[w];
+    for (uint64_t base = s0; base < s1; base += 32) {
+      const uint64_t k = base + lane;
+      const bool valid = k < s1;
+      const uint32_t x = valid ? nbr[k] : 0u;
+      const bool s = valid && is_selected(sel, x, row, mask, k);
+      const uint32_t bal = __ballot_sync(FULL, s);
+      if (s) reinterpret_cast<uint32_t*>(dst)[k_sel + __popc(bal & ((1u << lane) - 1u))] = x;
+      k_sel += __popc(bal);
+    }
+    __syncthreads();  // s_cnt is rewritten for the next row
+  }
+}
+
+// Row order by descending card: a histogram over 65,536 card buckets, a scan,
+// then a scatter.  Most rows share a few small cards, so lanes of a warp with
+// the same bucket combine their atomics (one per bucket and warp).
 __global__ void k_plan_hist(uint64_t n, const RowDesc* __restrict__ desc, uint32_t min_card,
                             uint32_t* __restrict__ hist) {
-  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = desc[r].card;
-    if (c >= min_card) atomicAdd(&hist[65535u - min(c, 65535u)], 1u);
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t r0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < n; r0 += step) {
+    const uint64_t r = r0 + lane;
+    const uint32_t c = r < n ? desc[r].card : 0u;
+    const bool take = r < n && c >= min_card;
+    const uint32_t bucket = take ? 65535u - min(c, 65535u) : 0xffffffffu;
+    const uint32_t peers = __match_any_sync(FULL, bucket);
+    if (take && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bucket], (uint32_t)__popc(peers));
   }
 }
 __global__ void k_plan_scatter(uint64_t n, const RowDesc* __restrict__ desc, uint32_t min_card,
                                uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
-  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = desc[r].card;
-    if (c >= min_card) order[atomicAdd(&cursor[65535u - min(c, 65535u)], 1u)] = (uint32_t)r;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t r0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < n; r0 += step) {
+    const uint64_t r = r0 + lane;
+    const uint32_t c = r < n ? desc[r].card : 0u;
+    const bool take = r < n && c >= min_card;
+    const uint32_t bucket = take ? 65535u - min(c, 65535u) : 0xffffffffu;
+    const uint32_t peers = __match_any_sync(FULL, bucket);
+    const uint32_t leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (take && lane == leader) base = atomicAdd(&cursor[bucket], (uint32_t)__popc(peers));
+    base = __shfl_sync(FULL, base, leader);
+    if (take) order[base + __popc(peers & ((1u << lane) - 1u))] = (uint32_t)r;
   }
 }
 
@@ -403,13 +628,17 @@ static int grid_for(uint64_t items, int per_block) {
   return (int)g;
 }
 
-cudaError_t launch_measure(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
-                           int sel, int layout, RowMeasure* meas, BuildTotals* totals, uint32_t* err,
-                           cudaStream_t st) {
+cudaError_t launch_measure(uint64_t n, uint64_t total, const uint64_t* off, const uint32_t* nbr,
+                           const uint8_t* mask, int sel, int layout, RowMeasure* meas, BuildTotals* totals,
+                           uint32_t* err, uint32_t* big, uint32_t* n_big, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_measure<<<grid_for(n, kBlock / 32), kBlock, 0, st>>>(n, off, nbr, mask, sel, layout, meas, totals, err);
+  k_measure<<<grid_for(n, kBlock / 32), kBlock, 0, st>>>(n, total, off, nbr, mask, sel, layout, meas, totals, err,
+                                                          big, n_big);
+  k_measure_big<<<2 * 152, kBigBlock, 0, st>>>(n, off, nbr, mask, sel, layout, meas, totals, err, big, n_big);
   return cudaGetLastError();
 }
+
+uint64_t big_row_capacity(uint64_t n, uint64_t total) { return std::min<uint64_t>(n, total / kBigRow + 1); }
 
 uint64_t scan_tmp_words(uint64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
@@ -421,9 +650,10 @@ cudaError_t launch_scan_units(uint64_t n, const RowMeasure* meas, uint32_t* off1
 
 cudaError_t launch_encode(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
                           int sel, const RowMeasure* meas, const uint32_t* off16, RowDesc* desc,
-                          uint4* arena, cudaStream_t st) {
+                          uint4* arena, const uint32_t* big, const uint32_t* n_big, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_encode<<<grid_for(n, kBlock / 32), kBlock, 0, st>>>(n, off, nbr, mask, sel, meas, off16, desc, arena);
+  k_encode_big<<<2 * 152, kBigBlock, 0, st>>>(off, nbr, mask, sel, meas, off16, arena, big, n_big);
   return cudaGetLastError();
 }
 

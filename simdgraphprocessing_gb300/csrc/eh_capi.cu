@@ -37,13 +37,19 @@ static uint64_t flattened_bytes(int layout, const RowDesc& d) {
 }
 
 eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask,
-                              int sel, int layout, cudaStream_t st, Matrix** out) {
+                              int sel, int layout, cudaStream_t st, Matrix** out, uint64_t total) {
   EH_CHECK_ARG(out != nullptr, "out is NULL");
   EH_CHECK_ARG(valid_layout(layout), "unknown layout %d", layout);
   EH_CHECK_ARG(sel >= 0 && sel <= 2, "unknown selection %d", sel);
   EH_CHECK_ARG(sel != EH_SELECT_MASK || d_mask != nullptr || n == 0, "EH_SELECT_MASK needs an edge mask");
   EH_CHECK_ARG(n < (1ull << 32), "n=%llu exceeds the u32 vertex id space", (unsigned long long)n);
   EH_CHECK_ARG(n == 0 || (d_off != nullptr), "offsets is NULL");
+  if (n && total == kTotalUnknown) {  // the neighbour array's length is offsets[n], on the device
+    cudaError_t ce = cudaMemcpyAsync(&total, d_off + n, sizeof(uint64_t), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return set_error(EH_ERR_CUDA, "offsets read: %s", cudaGetErrorString(ce));
+  }
+  EH_CHECK_ARG(n == 0 || total == 0 || d_nbr != nullptr, "nbrs is NULL");
   Matrix* m = new Matrix();
   m->n = n;
   m->layout = layout;
@@ -54,12 +60,15 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   uint32_t* err = nullptr;
   uint32_t* off16 = nullptr;
   uint32_t* tmp = nullptr;
+  uint32_t* big = nullptr;  // rows over 4,096 entries, then their count
+  const uint64_t big_cap = big_row_capacity(n, total);
   auto cleanup = [&]() {
     cudaFreeAsync(meas, st);
     cudaFreeAsync(tot, st);
     cudaFreeAsync(err, st);
     cudaFreeAsync(off16, st);
     cudaFreeAsync(tmp, st);
+    cudaFreeAsync(big, st);
   };
   auto fail = [&](eh_status s) {
     cleanup();
@@ -76,19 +85,23 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
       (e = cudaMallocAsync((void**)&tot, sizeof(BuildTotals), st)) != cudaSuccess ||
       (e = cudaMallocAsync((void**)&err, sizeof(uint32_t), st)) != cudaSuccess ||
       (e = cudaMallocAsync((void**)&off16, nn * sizeof(uint32_t), st)) != cudaSuccess ||
-      (e = cudaMallocAsync((void**)&tmp, scan_tmp_words(nn) * sizeof(uint32_t), st)) != cudaSuccess)
+      (e = cudaMallocAsync((void**)&tmp, scan_tmp_words(nn) * sizeof(uint32_t), st)) != cudaSuccess ||
+      (e = cudaMallocAsync((void**)&big, (big_cap + 1) * sizeof(uint32_t), st)) != cudaSuccess)
     return fail(e == cudaErrorMemoryAllocation ? set_error(EH_ERR_OUT_OF_MEMORY, "build scratch allocation failed")
                                                : cuda_fail(e, "cudaMallocAsync"));
   cudaMemsetAsync(tot, 0, sizeof(BuildTotals), st);
   cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
-  if ((e = launch_measure(n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, st)) != cudaSuccess)
+  cudaMemsetAsync(big + big_cap, 0, sizeof(uint32_t), st);
+  if ((e = launch_measure(n, total, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big, big + big_cap, st)) !=
+      cudaSuccess)
     return fail(cuda_fail(e, "measure kernel"));
   uint32_t herr = 0;
   cudaMemcpyAsync(&m->tot, tot, sizeof(BuildTotals), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail(cuda_fail(e, "measure"));
   if (herr) {
-    return fail(set_error(EH_ERR_INVALID_ARGUMENT, "adjacency rejected:%s%s%s",
+    return fail(set_error(EH_ERR_INVALID_ARGUMENT, "adjacency rejected:%s%s%s%s",
+                          (herr & ERRF_OFFSETS) ? " offsets fall or run past offsets[n];" : "",
                           (herr & ERRF_UNSORTED) ? " a row is not strictly ascending;" : "",
                           (herr & ERRF_RANGE) ? " a neighbour id is >= n;" : "",
                           (herr & ERRF_ROW_TOO_LONG) ? " a row has >= 2^28 selected entries;" : ""));
@@ -107,7 +120,8 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   m->result = reinterpret_cast<unsigned long long*>(m->counters + 16);
   m->device_bytes = nn * sizeof(RowDesc) + (m->arena_units + 1) * 16 + 128;
   cudaMemsetAsync(m->arena, 0, (m->arena_units + 1) * 16, st);
-  if ((e = launch_encode(n, d_off, d_nbr, d_mask, sel, meas, off16, m->desc, m->arena, st)) != cudaSuccess)
+  if ((e = launch_encode(n, d_off, d_nbr, d_mask, sel, meas, off16, m->desc, m->arena, big, big + big_cap, st)) !=
+      cudaSuccess)
     return fail(cuda_fail(e, "encode kernel"));
   cleanup();
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
@@ -391,7 +405,8 @@ eh_status eh_matrix_build_device(uint64_t n, const uint64_t* d_offsets, const ui
                                  const uint8_t* d_edge_mask, eh_selection sel, eh_layout layout,
                                  void* stream, eh_matrix_t* out) {
   Matrix* m = nullptr;
-  eh_status s = eh::build_device(n, d_offsets, d_nbrs, d_edge_mask, (int)sel, (int)layout, ST(stream), &m);
+  eh_status s = eh::build_device(n, d_offsets, d_nbrs, d_edge_mask, (int)sel, (int)layout, ST(stream), &m,
+                                 eh::kTotalUnknown);
   if (s == EH_OK) *out = reinterpret_cast<eh_matrix_t>(m);
   return s;
 }
@@ -405,8 +420,7 @@ eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* n
   const uint64_t m = offsets[n];
   EH_CHECK_ARG(m == 0 || nbrs != nullptr, "nbrs is NULL");
   EH_CHECK_ARG(sel != EH_SELECT_MASK || edge_mask != nullptr || m == 0, "EH_SELECT_MASK needs an edge mask");
-  for (uint64_t i = 0; i < n; i++)
-    EH_CHECK_ARG(offsets[i + 1] >= offsets[i], "offsets not monotone at row %llu", (unsigned long long)i);
+  // Offsets are checked on the device (each row must lie within [0, offsets[n])).
   cudaStream_t st = ST(stream);
   uint64_t* d_off = nullptr;
   uint32_t* d_nbr = nullptr;
@@ -422,7 +436,9 @@ eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* n
   cudaMemcpyAsync(d_off, offsets, (n + 1) * 8, cudaMemcpyHostToDevice, st);
   if (m) cudaMemcpyAsync(d_nbr, nbrs, m * 4, cudaMemcpyHostToDevice, st);
   if (d_mask && m) cudaMemcpyAsync(d_mask, edge_mask, m, cudaMemcpyHostToDevice, st);
-  eh_status s = eh_matrix_build_device(n, d_off, d_nbr, d_mask, sel, layout, stream, out);
+  Matrix* mx = nullptr;
+  eh_status s = eh::build_device(n, d_off, d_nbr, d_mask, (int)sel, (int)layout, st, &mx, m);
+  if (s == EH_OK) *out = reinterpret_cast<eh_matrix_t>(mx);
   cudaFreeAsync(d_off, st);
   cudaFreeAsync(d_nbr, st);
   if (d_mask) cudaFreeAsync(d_mask, st);

@@ -15,6 +15,7 @@ enum : uint32_t {
   ERRF_RANGE = 2u,         // a neighbour id >= n
   ERRF_ROW_TOO_LONG = 4u,  // a row exceeds the 2^30 element limit of RowDesc
   ERRF_PSHORT_PART = 8u,   // a pshort partition would exceed 65536 elements
+  ERRF_OFFSETS = 16u,      // offsets fall, or run past the neighbour array
 };
 
 // Per-row measurements produced by the build's first pass.
@@ -35,15 +36,18 @@ struct BuildTotals {  // accumulated with atomics by the measure pass
 };
 
 // eh_build.cu
-cudaError_t launch_measure(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
-                           int sel, int layout, RowMeasure* meas, BuildTotals* totals,
-                           uint32_t* err, cudaStream_t st);
+// big / n_big: the rows longer than 4,096 entries (measured and encoded by
+// whole CTAs), at most big_row_capacity(n, total) of them.
+cudaError_t launch_measure(uint64_t n, uint64_t total, const uint64_t* off, const uint32_t* nbr,
+                           const uint8_t* mask, int sel, int layout, RowMeasure* meas, BuildTotals* totals,
+                           uint32_t* err, uint32_t* big, uint32_t* n_big, cudaStream_t st);
+uint64_t big_row_capacity(uint64_t n, uint64_t total);
 cudaError_t launch_scan_units(uint64_t n, const RowMeasure* meas, uint32_t* off16, uint32_t* block_tmp,
                               uint64_t n_block_tmp, cudaStream_t st);
 uint64_t scan_tmp_words(uint64_t n);
 cudaError_t launch_encode(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask,
                           int sel, const RowMeasure* meas, const uint32_t* off16, RowDesc* desc,
-                          uint4* arena, cudaStream_t st);
+                          uint4* arena, const uint32_t* big, const uint32_t* n_big, cudaStream_t st);
 // Work plan: rows with card >= min_card sorted by descending card.
 // hist: 65536 + scan_tmp_words(65536) words; after the call hist[0..65536) holds
 // the bin starts and cursor[0..65536) the bin ends (bin b = card 65535 - b).

@@ -70,8 +70,11 @@ struct Matrix {
 };
 
 // eh_capi.cu
+// total = offsets[n] (the neighbour array's length), or kTotalUnknown to read it
+// from the device.
+constexpr uint64_t kTotalUnknown = ~0ull;
 eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask, int sel,
-                       int layout, cudaStream_t st, Matrix** out);
+                       int layout, cudaStream_t st, Matrix** out, uint64_t total);
 eh_status ensure_plan(Matrix* m, cudaStream_t st);
 eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaStream_t st);
 eh_status ensure_core(Matrix* m, cudaStream_t st);

@@ -109,6 +109,24 @@ def test_rejects_unsorted_rows_without_fault(eh):
     assert m.count_triangles() == 1
 
 
+def test_rejects_bad_offsets_without_fault(eh):
+    import torch
+    nbr = np.array([1, 2, 0, 2, 0, 1], np.uint32)
+    # falling offsets (row 1 would be [5, 2)), from host and from device buffers
+    bad = np.array([0, 5, 2, 6], np.uint64)
+    with pytest.raises(eh.EHError) as ei:
+        eh.Matrix.build(bad, nbr, selection="lower", layout="hybrid")
+    assert "offsets" in str(ei.value)
+    d_nbr = torch.from_numpy(nbr.view(np.int32)).cuda()
+    for off in (bad, np.array([0, 9, 9, 6], np.uint64)):  # the second runs past offsets[n]
+        d_off = torch.from_numpy(off.view(np.int64)).cuda()
+        with pytest.raises(eh.EHError):
+            eh.Matrix.build_device(3, d_off.data_ptr(), d_nbr.data_ptr(), selection="all", layout="uint")
+    good = torch.from_numpy(np.array([0, 2, 4, 6], np.uint64).view(np.int64)).cuda()
+    m = eh.Matrix.build_device(3, good.data_ptr(), d_nbr.data_ptr(), selection="lower", layout="hybrid")
+    assert m.count_triangles() == 1
+
+
 def test_empty_and_tiny_graphs(eh, oracle):
     for off, nbr in [(np.zeros(1, np.uint64), np.zeros(0, np.uint32)),
                      (np.zeros(5, np.uint64), np.zeros(0, np.uint32)),
