@@ -33,6 +33,7 @@ namespace eh {
 namespace {
 
 constexpr int NW = kCtaThreads / 32;
+constexpr uint32_t kCliqueWideMin = 1024;  // k <= 4 pivots above this run 1,024-thread CTAs
 
 __device__ __forceinline__ uint32_t ilog2p1_c(uint32_t x) { return 32u - __clz(x | 1u); }
 
@@ -143,13 +144,16 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
 // ---- CTA tiers: one pivot per CTA; masks in shared memory or a global slot ----
 // Per CTA working set (words): list[cmax] | masks[mask_off(cmax)] | stacks[NW][2 * (k-2) * W]
 // (stacks only for k >= 5); W = mask_len(cmax) is the DFS stack row length.
-template <bool GLOBAL>
-__global__ void __launch_bounds__(kCtaThreads, GLOBAL ? 2 : 8) k_clique_cta(CliqueArgs a, uint32_t pos_begin, uint32_t pos_end,
+// NT threads per CTA: 256, or 1,024 for the largest pivots at k <= 4, whose
+// masks leave room for one CTA per SM (more warps to hide latency).
+template <bool GLOBAL, int NT>
+__global__ void __launch_bounds__(NT, NT == 1024 ? 1 : (GLOBAL ? 2 : 8)) k_clique_cta(CliqueArgs a, uint32_t pos_begin, uint32_t pos_end,
                                                             uint32_t* counter, uint32_t cmax, uint32_t W,
                                                             uint32_t* gscratch, uint64_t slot_words) {
   extern __shared__ __align__(16) uint32_t dyn[];
   __shared__ uint32_t s_unit;
-  __shared__ uint32_t s_scan[kCtaThreads];
+  constexpr int NW = NT / 32;
+  __shared__ uint32_t s_scan[NT];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t* base = GLOBAL ? gscratch + (uint64_t)blockIdx.x * slot_words : dyn;
   uint32_t* list = base;
@@ -167,8 +171,8 @@ __global__ void __launch_bounds__(kCtaThreads, GLOBAL ? 2 : 8) k_clique_cta(Cliq
     const RowView A = load_view(a.desc, a.arena, row);
     const uint32_t c = A.card;
     const unsigned long long acc_before = acc;
-    cta_decode<kCtaThreads>(A, list, s_scan);
-    for (uint64_t x = threadIdx.x; x < mask_off(c); x += kCtaThreads) masks[x] = 0;
+    cta_decode<NT>(A, list, s_scan);
+    for (uint64_t x = threadIdx.x; x < mask_off(c); x += NT) masks[x] = 0;
     __syncthreads();
     // phase 1: warp per e builds M[e]
     for (uint32_t e = 1 + warp; e < c; e += NW) {
@@ -304,6 +308,7 @@ __global__ void __launch_bounds__(kCtaThreads, GLOBAL ? 2 : 8) k_clique_cta(Cliq
 
 uint64_t clique_slot_words(uint32_t cmax, uint32_t k) {
   const uint64_t W = mask_len(cmax);
+  // DFS stacks (k >= 5) are sized for the 256-thread CTAs that run those k.
   return (uint64_t)cmax + (uint64_t)mask_off(cmax) + (k >= 5 ? (uint64_t)NW * 2 * (k - 2) * W : 0);
 }
 
@@ -314,8 +319,9 @@ uint32_t clique_smem_cap(uint32_t k, int device) {
     cudaDeviceGetAttribute(&o, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (device >= 0 && device < 64) optin[device].store(o);
   }
-  // Leave room for the kernel's static shared memory (s_unit, s_scan).
-  const uint64_t budget = o > 2048 ? (uint64_t)o - 2048 : 0;
+  // Leave room for the kernel's static shared memory (s_unit, s_scan: 4,112 bytes
+  // in the 1,024-thread variant).
+  const uint64_t budget = o > 4608 ? (uint64_t)o - 4608 : 0;
   uint32_t lo = 32, hi = kCliqueSmemMax;
   while (lo < hi) {
     const uint32_t mid = (lo + hi + 1) / 2;
@@ -328,6 +334,7 @@ uint32_t clique_smem_cap(uint32_t k, int device) {
 // SMs x resident CTAs of the shared-memory clique kernel with `bytes` of
 // dynamic shared memory; looked up once per (device, size), so that launches
 // captured into a CUDA graph after a direct run make no occupancy query.
+template <int NT>
 static int resident_ctas(int dev, size_t bytes) {
   static std::mutex mu;
   static std::map<std::pair<int, size_t>, int> cache;
@@ -336,10 +343,35 @@ static int resident_ctas(int dev, size_t bytes) {
   if (it != cache.end()) return it->second;
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clique_cta<false>, kCtaThreads, bytes);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clique_cta<false, NT>, NT, bytes);
   const int g = std::max(sms, 1) * std::max(per, 1);
   cache[{dev, bytes}] = g;
   return g;
+}
+
+// Shared-memory launch with NT threads per CTA.
+template <int NT>
+static cudaError_t launch_shared(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
+                                 uint32_t cmax, uint32_t W, uint64_t slot, int grid, cudaStream_t st) {
+  const size_t bytes = slot * 4;
+  // Raise the kernel's dynamic shared-memory limit only when a launch needs more
+  // than any before it (so replays of captured launches never call this).
+  static std::atomic<int> set_bytes[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if ((int)bytes > set_bytes[dev].load()) {
+    cudaError_t e = cudaFuncSetAttribute(k_clique_cta<false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
+    if (e != cudaSuccess) return e;
+    int prev = set_bytes[dev].load();
+    while ((int)bytes > prev && !set_bytes[dev].compare_exchange_weak(prev, (int)bytes)) {
+    }
+  }
+  if (grid <= 0)  // fill the GPU: SMs x resident CTAs at this shared-memory size, at most one per pivot
+    grid = (int)std::min<uint64_t>(pos_end - pos_begin, (uint64_t)resident_ctas<NT>(dev, bytes));
+  k_clique_cta<false, NT><<<grid, NT, bytes, st>>>(a, pos_begin, pos_end, counter, cmax, W, nullptr, slot);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
@@ -354,29 +386,23 @@ cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t 
   if (pos_end <= pos_begin) return cudaSuccess;
   const uint32_t W = mask_len(cmax);
   const uint64_t slot = clique_slot_words(cmax, a.k);
+  const bool wide = a.k <= 4 && cmax > kCliqueWideMin;
   if (gscratch) {
-    k_clique_cta<true><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch, slot);
-  } else {
-    const size_t bytes = slot * 4;
-    // Raise the kernel's dynamic shared-memory limit only when a launch needs more
-    // than any before it (so replays of captured launches never call this).
-    static std::atomic<int> set_bytes[64];
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if ((int)bytes > set_bytes[dev].load()) {
-      cudaError_t e = cudaFuncSetAttribute(k_clique_cta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-      if (e != cudaSuccess) return e;
-      int prev = set_bytes[dev].load();
-      while ((int)bytes > prev && !set_bytes[dev].compare_exchange_weak(prev, (int)bytes)) {
-      }
+    if (wide) {
+      // One 1,024-thread CTA per SM in place of two 256-thread ones.
+      int sms = 0, dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      grid = std::max(1, std::min(grid, sms));
+      k_clique_cta<true, 1024><<<grid, 1024, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch, slot);
+    } else {
+      k_clique_cta<true, kCtaThreads><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W,
+                                                                    gscratch, slot);
     }
-    if (grid <= 0) {  // fill the GPU: SMs x resident CTAs at this shared-memory size, at most one per pivot
-      grid = (int)std::min<uint64_t>(pos_end - pos_begin, (uint64_t)resident_ctas(dev, bytes));
-    }
-    k_clique_cta<false><<<grid, kCtaThreads, bytes, st>>>(a, pos_begin, pos_end, counter, cmax, W, nullptr, slot);
+    return cudaGetLastError();
   }
-  return cudaGetLastError();
+  return wide ? launch_shared<1024>(a, pos_begin, pos_end, counter, cmax, W, slot, grid, st)
+              : launch_shared<kCtaThreads>(a, pos_begin, pos_end, counter, cmax, W, slot, grid, st);
 }
 
 }  // namespace eh
