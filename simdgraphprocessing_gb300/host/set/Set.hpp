@@ -23,12 +23,31 @@ class Set {
         type(type_in) {}
   explicit Set(uint8_t* data_in)
       : data(data_in), cardinality(0), number_of_bytes(0), density(0.0), type(T::get_type()) {}
+  // A zeroed buffer of the given size (Set.hpp:47-56; like the reference, the
+  // buffer belongs to the caller from here on).
+  explicit Set(size_t number_of_bytes_in)
+      : data(new uint8_t[number_of_bytes_in]()), cardinality(0), number_of_bytes(number_of_bytes_in),
+        density(0.0), type(T::get_type()) {}
   Set(uint8_t* data_in, size_t number_of_bytes_in)
       : data(data_in), cardinality(0), number_of_bytes(number_of_bytes_in), density(0.0), type(T::get_type()) {}
   template <class U>
   Set(Set<U> in)
       : data(in.data), cardinality(in.cardinality), number_of_bytes(in.number_of_bytes), density(in.density),
         type(in.type) {}
+  template <class U>
+  Set(Set<U>* in)
+      : data(in->data), cardinality(in->cardinality), number_of_bytes(in->number_of_bytes), density(in->density),
+        type(in->type) {}
+
+  // Copies another set's bytes and metadata (Set::copy_from, used by n_path).
+  template <class U>
+  void copy_from(const Set<U>& in) {
+    std::memcpy(data, in.data, in.number_of_bytes);
+    cardinality = in.cardinality;
+    number_of_bytes = in.number_of_bytes;
+    density = in.density;
+    type = in.type;
+  }
 
   template <typename F>
   void foreach(F f) const {
@@ -45,5 +64,7 @@ class Set {
     return Set<T>(set_data + std::get<0>(f), cardinality_in, std::get<1>(f), std::get<2>(f));
   }
 };
+
+#include "ops.hpp"
 
 #endif

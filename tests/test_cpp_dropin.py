@@ -44,6 +44,24 @@ def _build_driver(tmp_path, eh, name="dropin_apps"):
     return exe
 
 
+def test_host_set_ops(tmp_path):
+    """ops::set_intersect / set_union / set_difference of the drop-in headers
+    (host-side compat for code that combines rows read back with get_row)."""
+    exe = str(tmp_path / "set_ops")
+    cmd = ["g++", "-std=c++11", "-O1", "-fopenmp", "-I", HOST, "-I", CUDA_INC,
+           os.path.join(ROOT, "tests", "cpp", "set_ops.cpp"), "-o", exe]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout[-3000:]
+    out = subprocess.run([exe], stdout=subprocess.PIPE, text=True, check=True).stdout
+    got = {l.split()[0]: [int(x) for x in l.split()[1:]] for l in out.splitlines()}
+    both = [5, 9, 127, 70001]
+    for k in ("uu", "up", "pb", "bb", "pp"):
+        assert got[k] == [len(both)] + both, k
+    assert got["pp_full"] == [1, 70000]       # the shared full 2^16 block counts 0 (u16)
+    assert got["up_full"][0] == 65537          # mixed layouts count it
+    assert got["diff"] == [3, 6, 128, 90000]  # bits set by the second union only
+
+
 def test_dropin_driver_compiles(tmp_path, eh):
     _build_driver(tmp_path, eh)
     _build_driver(tmp_path, eh, "dropin_directed")
