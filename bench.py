@@ -411,6 +411,10 @@ def run_cliques(a):
         off, nbr = g.csr()[:2]
         low = eh.Matrix.build(off, nbr, "lower", a.layout, stream=stream)
         full = eh.Matrix.build(off, nbr, "all", a.layout, stream=stream)
+        # Work shapes: the pruned matrix tuned on triangles (its dense core also
+        # serves the clique kernels), the full one on lollipops.
+        low.tune(stream=stream)
+        full.tune(stream=stream)
         res = {"graph": name, "pruned_edges": low.info()["cardinality"], "layout": a.layout,
                "bitset_rows_lower": low.info()["num_bitset_rows"]}
         c4 = low.count_cliques(4, stream=stream)

@@ -276,10 +276,11 @@ typedef struct eh_tuning {
   float ms;               /* median triangle-count time with the chosen shape        */
   uint32_t configs_tried;
 } eh_tuning;
-/* Times the triangle count on this matrix for a small set of work shapes,
- * coordinate by coordinate, keeps the fastest for later counts, and caches it
- * per (GPU, layout, size bucket) in the process (and in the file named by
- * EH_TUNE_CACHE, if set).  Matrix built with EH_SELECT_LOWER. */
+/* Times the triangle count (EH_SELECT_LOWER) or the lollipop count
+ * (EH_SELECT_ALL) on this matrix for a small set of work shapes, coordinate by
+ * coordinate, keeps the fastest for later counts, and caches it per (GPU,
+ * layout, selection, size bucket) in the process (and in the file named by
+ * EH_TUNE_CACHE, if set). */
 eh_status eh_matrix_tune(eh_matrix_t m, void* stream, eh_tuning* result);
 
 /* ------------------------------------------------------------------------- */

@@ -58,8 +58,8 @@ std::string tune_key(const Matrix* m, bool batch) {
   while ((1ull << (lc + 1)) <= m->tot.cardinality) lc++;
   while ((1ull << (lr + 1)) <= m->n) lr++;
   char buf[512];
-  snprintf(buf, sizeof(buf), "%.200s|sm%d|layout%d|card2^%d|rows2^%d|%s", prop.name, prop.multiProcessorCount, m->layout,
-           lc, lr, batch ? "batch" : "single");
+  snprintf(buf, sizeof(buf), "%.200s|sm%d|layout%d|sel%d|card2^%d|rows2^%d|%s", prop.name, prop.multiProcessorCount,
+           m->layout, m->selection, lc, lr, batch ? "batch" : "single");
   std::string k = buf;
   for (char& ch : k)
     if (ch == ' ') ch = '_';
@@ -113,9 +113,12 @@ eh_status time_shape(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs,
   cudaEventCreate(&e1);
   std::vector<float> t;
   eh_status s = EH_OK;
+  // A matrix of full rows (EH_SELECT_ALL) is tuned on the lollipop count, the
+  // other use of the same pivot kernels; pruned matrices on the triangle count.
+  const bool lolli = m->selection == EH_SELECT_ALL && !graph_rows;
   for (int r = 0; r <= reps && s == EH_OK; r++) {
     cudaEventRecord(e0, st);
-    s = launch_triangle_count(m, out, graph_rows, num_graphs, st);
+    s = lolli ? launch_lollipop_count(m, out, st) : launch_triangle_count(m, out, graph_rows, num_graphs, st);
     cudaEventRecord(e1, st);
     cudaEventSynchronize(e1);
     float x = 0;
@@ -227,8 +230,9 @@ eh_status eh_matrix_tune(eh_matrix_t mh, void* stream, eh_tuning* result) {
   if (!mh) return set_error(EH_ERR_INVALID_ARGUMENT, "matrix is NULL");
   eh::Matrix* m = reinterpret_cast<eh::Matrix*>(mh);
   cudaSetDevice(m->device);
-  if (m->selection != EH_SELECT_LOWER)
-    return set_error(EH_ERR_UNSUPPORTED, "tuning times the triangle count: build the matrix with EH_SELECT_LOWER");
+  if (m->selection == EH_SELECT_MASK)
+    return set_error(EH_ERR_UNSUPPORTED,
+                     "tuning times the triangle count (EH_SELECT_LOWER) or the lollipop count (EH_SELECT_ALL)");
   return eh::tune(m, nullptr, 0, reinterpret_cast<cudaStream_t>(stream), result);
 }
 

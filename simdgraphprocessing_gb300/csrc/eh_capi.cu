@@ -371,6 +371,14 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
   return EH_OK;
 }
 
+eh_status launch_lollipop_count(Matrix* m, unsigned long long* out, cudaStream_t st) {
+  eh_status s = ensure_plan(m, st);
+  if (s != EH_OK) return s;
+  PivotArgs a = pivot_args(m, out);
+  CU(launch_lollipops(a, m->plan.units, m->plan.n_units, m->grid, st), "lollipop kernel");
+  return EH_OK;
+}
+
 eh_status launch_triangle_count(Matrix* m, unsigned long long* out, const uint32_t* graph_rows, uint32_t num_graphs,
                                 cudaStream_t st, Workspace* ws) {
   if (m->selection != EH_SELECT_LOWER)
@@ -601,12 +609,7 @@ eh_status eh_count_triangles(eh_matrix_t mh, uint64_t* count, void* stream) {
 eh_status eh_count_lollipops_async(eh_matrix_t mh, uint64_t* d_count, void* stream) {
   CHECK_MATRIX(mh);
   EH_CHECK_ARG(d_count, "d_count is NULL");
-  Matrix* m = MX(mh);
-  eh_status s = eh::ensure_plan(m, ST(stream));
-  if (s != EH_OK) return s;
-  eh::PivotArgs a = eh::pivot_args(m, reinterpret_cast<unsigned long long*>(d_count));
-  CU(eh::launch_lollipops(a, m->plan.units, m->plan.n_units, m->grid, ST(stream)), "lollipop kernel");
-  return EH_OK;
+  return eh::launch_lollipop_count(MX(mh), reinterpret_cast<unsigned long long*>(d_count), ST(stream));
 }
 
 eh_status eh_count_lollipops(eh_matrix_t mh, uint64_t* count, void* stream) {

@@ -86,6 +86,7 @@ PivotArgs pivot_args(Matrix* m, unsigned long long* out);
 // already exist when ws != null (launches with a workspace never allocate it).
 eh_status launch_triangle_count(Matrix* m, unsigned long long* out, const uint32_t* graph_rows, uint32_t num_graphs,
                                 cudaStream_t st, Workspace* ws = nullptr);
+eh_status launch_lollipop_count(Matrix* m, unsigned long long* out, cudaStream_t st);
 eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const uint32_t* graph_rows,
                          uint32_t num_graphs, cudaStream_t st, Workspace* ws = nullptr);
 

@@ -82,3 +82,13 @@ def test_single_matrix_tuning_keeps_counts(eh, oracle):
     assert shape["light_max"] in (32, 64, 96) and shape["unit_span"] in (32, 64, 128, 256, 512, 1024, 2048)
     assert m.count_triangles() == want
     assert m.count_cliques(4) == oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.HYBRID).cliques(4)
+
+
+def test_full_row_matrix_tunes_on_lollipops(eh, oracle):
+    off, nbr = eh.graph("rmat", 14, scale=12, edges=40000).csr()[:2]
+    m = eh.Matrix.build(off, nbr, "all", "hybrid")
+    want = oracle.Matrix(off, nbr, oracle.SELECT_ALL, oracle.HYBRID).lollipops()
+    assert m.count_lollipops() == want
+    shape = m.tune()
+    assert shape["configs_tried"] >= 1
+    assert m.count_lollipops() == want
