@@ -119,6 +119,7 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   // Words 0..15: work-queue counters; 16..17: the u64 result of the synchronous calls.
   m->result = reinterpret_cast<unsigned long long*>(m->counters + 16);
   m->device_bytes = nn * sizeof(RowDesc) + (m->arena_units + 1) * 16 + 128;
+  cudaMemsetAsync(m->counters, 0, 128, st);
   cudaMemsetAsync(m->arena, 0, (m->arena_units + 1) * 16, st);
   if ((e = launch_encode(n, d_off, d_nbr, d_mask, sel, meas, off16, m->desc, m->arena, big, big + big_cap, st)) !=
       cudaSuccess)
@@ -295,10 +296,18 @@ PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
   return a;
 }
 
+// Copies the result back and checks the kernels' device error flags
+// (counters[15]; e.g. a bulk copy whose bounded wait ran out), which are
+// cleared when reported.
 static eh_status finish_sync(Matrix* m, unsigned long long* d_res, uint64_t* count, cudaStream_t st) {
-  (void)m;
+  uint32_t flags = 0;
   CU(cudaMemcpyAsync(count, d_res, sizeof(uint64_t), cudaMemcpyDeviceToHost, st), "result copy");
+  CU(cudaMemcpyAsync(&flags, m->counters + 15, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "flag copy");
   CU(cudaStreamSynchronize(st), "count");
+  if (flags) {
+    CU(cudaMemsetAsync(m->counters + 15, 0, sizeof(uint32_t), st), "flag reset");
+    return set_error(EH_ERR_DEVICE_CHECK, "a device-side wait ran out (flags 0x%x); the count is not valid", flags);
+  }
   return EH_OK;
 }
 

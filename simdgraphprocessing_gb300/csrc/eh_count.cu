@@ -43,8 +43,11 @@ struct __align__(16) HeavySmem {
   unsigned long long abits[kCoreAndMax / 64];  // pivot ∩ [0, min(core_k, kCoreAndMax)) as bits
   uint32_t list[kCtaListCap];
   uint32_t scan[kCtaThreads];
+  uint64_t bar;  // completion of the unit's bulk copy
   uint32_t unit;
 };
+// Device error flag (PivotArgs::counters[kErrWord]): a bulk copy's wait ran out.
+constexpr uint32_t kErrWord = 15, kErrBulkWait = 1u;
 
 // Warp, CTA, then one u64 atomic per CTA into the single count.
 __device__ __forceinline__ void cta_add(unsigned long long acc, const PivotArgs& a) {
@@ -130,28 +133,40 @@ __global__ void __launch_bounds__(kCtaThreads, 6) k_pivots_heavy(PivotArgs a, co
   __shared__ HeavySmem s;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long acc = 0;
+  uint32_t phase = 0;
+  if (threadIdx.x == 0) mbar_init(&s.bar);
 
   // ---- heavy pivots: CTA-wide units ----
   for (;;) {
     if (threadIdx.x == 0) s.unit = atomicAdd(&a.counters[0], 1u);
-    __syncthreads();
+    __syncthreads();  // also: every thread is done with the previous unit's staging
     const uint32_t unit = s.unit;
     if (unit >= n_units) break;
     const uint2 uu = units[unit];
     const uint32_t i = a.order[uu.x];
     RowView A = load_view(a.desc, a.arena, i);
     const uint32_t* L;
+    // uint pivots and bitset words are staged by one bulk (TMA) copy: row
+    // payloads start on 16-byte boundaries and are padded to 16 bytes.
+    const bool bulk_list = uu.x >= a.n_giant && A.type == TY_UINT;
+    const bool bulk_words = A.type == TY_BITSET && A.len <= kCtaWordCap;
+    if (bulk_list || bulk_words) {
+      if (threadIdx.x == 0) {
+        if (bulk_list) bulk_copy_g2s(s.list, A.p, (4 * A.card + 15) & ~15u, &s.bar);
+        else bulk_copy_g2s(s.words, A.p, (8 * A.len + 15) & ~15u, &s.bar);
+      }
+      if (!mbar_wait(&s.bar, phase) && threadIdx.x == 0) atomicOr(&a.counters[kErrWord], kErrBulkWait);
+      phase ^= 1u;
+    }
     if (uu.x < a.n_giant) {
       L = (A.type == TY_UINT) ? static_cast<const uint32_t*>(A.p) : a.giant_lists + a.giant_off[uu.x];
+    } else if (bulk_list) {
+      L = s.list;
     } else {
       cta_decode<kCtaThreads>(A, s.list, s.scan);
       L = s.list;
     }
-    if (A.type == TY_BITSET && A.len <= kCtaWordCap) {
-      const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
-      for (uint32_t k = threadIdx.x; k < A.len; k += kCtaThreads) s.words[k] = w[k];
-      A.p = s.words;
-    }
+    if (bulk_words) A.p = s.words;
     // The core path is skipped for pshort pivots of >= 65,536 entries, where the
     // reference's u16 partition count can drop a block (see pshort_pair_drop).
     const bool use_core = a.core_k && !(A.type == TY_PSHORT && A.card >= 65536u);

@@ -51,6 +51,43 @@ __device__ __forceinline__ RowView load_view(const RowDesc* __restrict__ desc,
 
 constexpr uint32_t FULL = 0xffffffffu;
 
+// ---- Bulk (TMA) copies from global to shared memory, completing on an mbarrier ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// One thread: initialise a CTA-local mbarrier expecting one arrival per phase.
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One thread: order this CTA's earlier shared-memory accesses (made visible to
+// it by a __syncthreads) before the async proxy's writes, arm `bar` for `bytes`
+// and start the copy.  dst and src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Every thread: wait for phase `parity` of `bar` to complete.  The wait is
+// bounded; false means it ran out (the caller records an error and moves on).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < (1u << 22); i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t x) { return __reduce_add_sync(FULL, x); }
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x) {
   for (int d = 16; d; d >>= 1) x += __shfl_xor_sync(FULL, x, d);

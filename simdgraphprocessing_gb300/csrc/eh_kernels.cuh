@@ -71,7 +71,7 @@ struct PivotArgs {
   uint32_t n_giant;        // order[0, n_giant) have decoded lists in giant_lists
   const uint32_t* giant_lists;
   const unsigned long long* giant_off;
-  uint32_t* counters;      // [0] next heavy unit, [1] next light chunk
+  uint32_t* counters;      // [0] next heavy unit, [1] next light chunk, [15] device error flags
   unsigned long long* out; // result; in batch mode out[num_graphs]
   uint32_t unit_span;      // pivot positions e per heavy unit
   const uint32_t* graph_rows;  // batch mode: graph g owns rows [graph_rows[g], graph_rows[g+1]); else null

@@ -221,6 +221,7 @@ eh_status eh_server_create(const eh_server_config* cfg, eh_server_t* out) {
     if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc((void**)&sl.ws.counters, 64) != cudaSuccess ||
+        cudaMemset(sl.ws.counters, 0, 64) != cudaSuccess ||
         cudaMalloc((void**)&sl.d_out, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMallocHost((void**)&sl.h_out, sizeof(uint64_t)) != cudaSuccess) {
       eh_server_free(reinterpret_cast<eh_server_t>(s));
