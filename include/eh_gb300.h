@@ -353,6 +353,16 @@ eh_status eh_server_stats(eh_server_t s, eh_server_counters* out);
 /* Finishes queued and running queries, stops the dispatcher, frees everything. */
 void eh_server_free(eh_server_t s);
 
+/* ------------------------------------------------------------------------- */
+/* Diagnostics (no reference counterpart).                                     */
+/* ------------------------------------------------------------------------- */
+/* Runs one kernel that waits on an mbarrier nothing arrives on, with the
+ * bounded wait the bulk-copy staging uses, limited to `tries` polls
+ * (1..65536); *timed_out = 1 when the wait gave up and the kernel reported it
+ * (the expected outcome).  Shows that a stuck device-side wait ends with a
+ * status instead of a hang. */
+eh_status eh_selftest_bounded_wait(uint32_t tries, uint32_t* timed_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -126,6 +126,7 @@ def load(build_if_missing=True):
         "eh_symbiosity": (I, [P, P, C.c_double, C.POINTER(U64), P]),
         "eh_symbiosity_async": (I, [P, P, C.c_double, P, P]),
         "eh_bfs_path_length": (I, [P, U32, U64, C.POINTER(U64), C.POINTER(U64), P]),
+        "eh_selftest_bounded_wait": (I, [U32, C.POINTER(U32)]),
         "eh_list_triangles": (I, [P, P, U64, P, P]),
         "eh_matrix_tune": (I, [P, P, C.POINTER(Tuning)]),
         "eh_batch_build": (I, [U32, P, U64, P, P, I, P, C.POINTER(P)]),

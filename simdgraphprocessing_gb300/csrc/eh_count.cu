@@ -155,7 +155,12 @@ __global__ void __launch_bounds__(kCtaThreads, 6) k_pivots_heavy(PivotArgs a, co
         if (bulk_list) bulk_copy_g2s(s.list, A.p, (4 * A.card + 15) & ~15u, &s.bar);
         else bulk_copy_g2s(s.words, A.p, (8 * A.len + 15) & ~15u, &s.bar);
       }
-      if (!mbar_wait(&s.bar, phase) && threadIdx.x == 0) atomicOr(&a.counters[kErrWord], kErrBulkWait);
+      if (!mbar_wait(&s.bar, phase)) {
+        // Record the failure, then give the copy in flight a second bounded
+        // wait before the buffer is used or the CTA exits.
+        if (threadIdx.x == 0) atomicOr(&a.counters[kErrWord], kErrBulkWait);
+        mbar_wait(&s.bar, phase);
+      }
       phase ^= 1u;
     }
     if (uu.x < a.n_giant) {

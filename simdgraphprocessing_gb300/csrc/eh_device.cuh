@@ -75,8 +75,8 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
 
 // Every thread: wait for phase `parity` of `bar` to complete.  The wait is
 // bounded; false means it ran out (the caller records an error and moves on).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < (1u << 22); i++) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_tries = 1u << 22) {
+  for (uint32_t i = 0; i < max_tries; i++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

@@ -480,3 +480,38 @@ extern "C" eh_status eh_bfs_path_length(eh_matrix_t mh, uint32_t start, uint64_t
   if (reached) *reached = r;
   return done(EH_OK);
 }
+
+// ---- diagnostics: the bounded mbarrier wait used by the bulk-copy staging ----
+namespace eh {
+namespace {
+// Waits on an mbarrier that nothing arrives on; the wait must give up after
+// `tries` polls and the kernel report it instead of hanging.
+__global__ void k_selftest_bounded_wait(uint32_t tries, uint32_t* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar);
+  __syncthreads();
+  const bool done = mbar_wait(&bar, 0, tries);
+  if (threadIdx.x == 0) *status = done ? 1u : 2u;
+}
+}  // namespace
+}  // namespace eh
+
+extern "C" eh_status eh_selftest_bounded_wait(uint32_t tries, uint32_t* timed_out) {
+  using namespace eh;
+  EH_CHECK_ARG(timed_out, "timed_out is NULL");
+  EH_CHECK_ARG(tries > 0 && tries <= (1u << 16), "tries must be in [1, 65536]");
+  uint32_t* d = nullptr;
+  cudaError_t e = cudaMalloc((void**)&d, sizeof(uint32_t));
+  if (e != cudaSuccess) return cuda_err(e, "selftest allocation");
+  uint32_t h = 0;
+  e = cudaMemset(d, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) {
+    k_selftest_bounded_wait<<<1, 32>>>(tries, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_err(e, "selftest");
+  *timed_out = h == 2u;
+  return h ? EH_OK : set_error(EH_ERR_DEVICE_CHECK, "self-test kernel did not report");
+}

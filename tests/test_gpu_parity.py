@@ -229,3 +229,14 @@ def test_clique_size_limits(eh):
     full = eh.Matrix.build(off, nbr, selection="all", layout="hybrid")
     with pytest.raises(eh.EHError):
         full.count_cliques(4)
+
+
+def test_device_waits_are_bounded(eh):
+    """A device-side wait that nothing completes gives up after its poll limit
+    and reports it (no hang, no fault); the context stays usable."""
+    import ctypes as C
+    flag = C.c_uint32(0)
+    eh.check(eh.load().eh_selftest_bounded_wait(64, C.byref(flag)))
+    assert flag.value == 1
+    off, nbr = csr(eh, "rmat10")
+    assert eh.Matrix.build(off, nbr, selection="lower").count_triangles() > 0
