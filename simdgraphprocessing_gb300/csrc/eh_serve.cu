@@ -48,7 +48,7 @@ struct Slot {
   cudaEvent_t ev = nullptr;
   Workspace ws;
   unsigned long long* d_out = nullptr;
-  uint64_t* h_out = nullptr;  // pinned
+  uint64_t* h_out = nullptr;  // pinned: [0] the count, [1] the query's device error flags
   uint64_t ticket = 0;
   bool busy = false;
 };
@@ -105,6 +105,10 @@ eh_status launch_query(Server* s, Slot& sl, const Query& q) {
   }
   if (st != EH_OK) return st;
   cudaMemcpyAsync(sl.h_out, sl.d_out, sizeof(uint64_t), cudaMemcpyDeviceToHost, sl.st);
+  // The pivot kernels' flags word (a bounded wait that ran out), cleared for the slot's next query.
+  sl.h_out[1] = 0;
+  cudaMemcpyAsync(sl.h_out + 1, sl.ws.counters + 15, sizeof(uint32_t), cudaMemcpyDeviceToHost, sl.st);
+  cudaMemsetAsync(sl.ws.counters + 15, 0, sizeof(uint32_t), sl.st);
   cudaEventRecord(sl.ev, sl.st);
   return EH_OK;
 }
@@ -129,7 +133,7 @@ void dispatch_loop(Server* s) {
       Query& q = s->queries[sl.ticket];
       q.done_ns = now_ns();
       q.count = *sl.h_out;
-      q.status = e == cudaSuccess ? EH_OK : EH_ERR_CUDA;
+      q.status = e != cudaSuccess ? EH_ERR_CUDA : sl.h_out[1] ? EH_ERR_DEVICE_CHECK : EH_OK;
       q.done = true;
       sl.busy = false;
       s->completed++;
@@ -223,7 +227,7 @@ eh_status eh_server_create(const eh_server_config* cfg, eh_server_t* out) {
         cudaMalloc((void**)&sl.ws.counters, 64) != cudaSuccess ||
         cudaMemset(sl.ws.counters, 0, 64) != cudaSuccess ||
         cudaMalloc((void**)&sl.d_out, sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMallocHost((void**)&sl.h_out, sizeof(uint64_t)) != cudaSuccess) {
+        cudaMallocHost((void**)&sl.h_out, 2 * sizeof(uint64_t)) != cudaSuccess) {
       eh_server_free(reinterpret_cast<eh_server_t>(s));
       return set_error(EH_ERR_OUT_OF_MEMORY, "server slot allocation failed");
     }
