@@ -171,7 +171,8 @@ struct Totals {
   }
 };
 
-__global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, uint64_t total, const uint64_t* __restrict__ off,
+__global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, uint64_t total, uint64_t r_begin, uint64_t r_end,
+                                                    const uint64_t* __restrict__ off,
                                                     const uint32_t* __restrict__ nbr,
                                                     const uint8_t* __restrict__ mask, int sel,
                                                     int layout, RowMeasure* __restrict__ meas,
@@ -182,16 +183,17 @@ __global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, uint64_t total, 
   const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
   uint32_t flags = 0;
   Totals t;  // lane 0's running totals for this warp's rows (one atomic each at the end)
-  // Rows are dealt to warps round-robin (row = warp + i * warps, so that the
-  // degree-ordered hubs at the front spread over the grid); a warp loads the
-  // offsets of its next 32 rows at once (lane q: its q-th row), then measures
-  // them one by one.
-  for (uint64_t row0 = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row0 < n; row0 += nw * 32) {
+  // Rows [r_begin, r_end) are dealt to warps round-robin (row = r_begin + warp
+  // + i * warps, so that the degree-ordered hubs at the front spread over the
+  // grid); a warp loads the offsets of its next 32 rows at once (lane q: its
+  // q-th row), then measures them one by one.
+  for (uint64_t row0 = r_begin + (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row0 < r_end;
+       row0 += nw * 32) {
     const uint64_t my = row0 + lane * nw;
-    const uint64_t my_b = my < n ? off[my] : 0, my_e = my < n ? off[my + 1] : 0;
+    const uint64_t my_b = my < r_end ? off[my] : 0, my_e = my < r_end ? off[my + 1] : 0;
     for (uint32_t q = 0; q < 32; q++) {
       const uint64_t row = row0 + q * nw;
-      if (row >= n) break;
+      if (row >= r_end) break;
       uint64_t b = __shfl_sync(FULL, my_b, q), e = __shfl_sync(FULL, my_e, q);
       if (e < b || e > total) {  // offsets must rise monotonically within the nbr array
         flags |= ERRF_OFFSETS;
@@ -628,12 +630,19 @@ static int grid_for(uint64_t items, int per_block) {
   return (int)g;
 }
 
-cudaError_t launch_measure(uint64_t n, uint64_t total, const uint64_t* off, const uint32_t* nbr,
-                           const uint8_t* mask, int sel, int layout, RowMeasure* meas, BuildTotals* totals,
-                           uint32_t* err, uint32_t* big, uint32_t* n_big, cudaStream_t st) {
+cudaError_t launch_measure_rows(uint64_t n, uint64_t total, uint64_t r_begin, uint64_t r_end, const uint64_t* off,
+                                const uint32_t* nbr, const uint8_t* mask, int sel, int layout, RowMeasure* meas,
+                                BuildTotals* totals, uint32_t* err, uint32_t* big, uint32_t* n_big, cudaStream_t st) {
+  if (r_end <= r_begin) return cudaSuccess;
+  k_measure<<<grid_for(r_end - r_begin, kBlock / 32), kBlock, 0, st>>>(n, total, r_begin, r_end, off, nbr, mask, sel,
+                                                                        layout, meas, totals, err, big, n_big);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_measure_big(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask, int sel,
+                               int layout, RowMeasure* meas, BuildTotals* totals, uint32_t* err, const uint32_t* big,
+                               const uint32_t* n_big, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_measure<<<grid_for(n, kBlock / 32), kBlock, 0, st>>>(n, total, off, nbr, mask, sel, layout, meas, totals, err,
-                                                          big, n_big);
   k_measure_big<<<2 * 152, kBigBlock, 0, st>>>(n, off, nbr, mask, sel, layout, meas, totals, err, big, n_big);
   return cudaGetLastError();
 }

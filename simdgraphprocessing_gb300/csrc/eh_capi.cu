@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -36,8 +37,57 @@ static uint64_t flattened_bytes(int layout, const RowDesc& d) {
   return inner + (is_hybrid(layout) ? 8 : 0);
 }
 
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_device_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+cudaStream_t g_upload_stream[kMaxDevices] = {};
+}  // namespace
+
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> g(g_device_mu);
+    if (!g_pool[dev]) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t created = nullptr;
+      if ((e = cudaMemPoolCreate(&created, &props)) != cudaSuccess) return e;
+      uint64_t keep = kPoolKeep;
+      if ((e = cudaMemPoolSetAttribute(created, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+        cudaMemPoolDestroy(created);
+        return e;
+      }
+      g_pool[dev] = created;
+    }
+    pool = g_pool[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
+cudaError_t upload_stream(cudaStream_t* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(g_device_mu);
+  if (!g_upload_stream[dev] &&
+      (e = cudaStreamCreateWithFlags(&g_upload_stream[dev], cudaStreamNonBlocking)) != cudaSuccess) {
+    g_upload_stream[dev] = nullptr;
+    return e;
+  }
+  *out = g_upload_stream[dev];
+  return cudaSuccess;
+}
+
 eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask,
-                              int sel, int layout, cudaStream_t st, Matrix** out, uint64_t total) {
+                       int sel, int layout, cudaStream_t st, Matrix** out, uint64_t total, const UploadChunks* up) {
   EH_CHECK_ARG(out != nullptr, "out is NULL");
   EH_CHECK_ARG(valid_layout(layout), "unknown layout %d", layout);
   EH_CHECK_ARG(sel >= 0 && sel <= 2, "unknown selection %d", sel);
@@ -81,20 +131,31 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   };
   cudaError_t e;
   const uint64_t nn = n ? n : 1;
-  if ((e = cudaMallocAsync((void**)&meas, nn * sizeof(RowMeasure), st)) != cudaSuccess ||
-      (e = cudaMallocAsync((void**)&tot, sizeof(BuildTotals), st)) != cudaSuccess ||
-      (e = cudaMallocAsync((void**)&err, sizeof(uint32_t), st)) != cudaSuccess ||
-      (e = cudaMallocAsync((void**)&off16, nn * sizeof(uint32_t), st)) != cudaSuccess ||
-      (e = cudaMallocAsync((void**)&tmp, scan_tmp_words(nn) * sizeof(uint32_t), st)) != cudaSuccess ||
-      (e = cudaMallocAsync((void**)&big, (big_cap + 1) * sizeof(uint32_t), st)) != cudaSuccess)
+  if ((e = pool_alloc((void**)&meas, nn * sizeof(RowMeasure), st)) != cudaSuccess ||
+      (e = pool_alloc((void**)&tot, sizeof(BuildTotals), st)) != cudaSuccess ||
+      (e = pool_alloc((void**)&err, sizeof(uint32_t), st)) != cudaSuccess ||
+      (e = pool_alloc((void**)&off16, nn * sizeof(uint32_t), st)) != cudaSuccess ||
+      (e = pool_alloc((void**)&tmp, scan_tmp_words(nn) * sizeof(uint32_t), st)) != cudaSuccess ||
+      (e = pool_alloc((void**)&big, (big_cap + 1) * sizeof(uint32_t), st)) != cudaSuccess)
     return fail(e == cudaErrorMemoryAllocation ? set_error(EH_ERR_OUT_OF_MEMORY, "build scratch allocation failed")
                                                : cuda_fail(e, "cudaMallocAsync"));
   cudaMemsetAsync(tot, 0, sizeof(BuildTotals), st);
   cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
   cudaMemsetAsync(big + big_cap, 0, sizeof(uint32_t), st);
-  if ((e = launch_measure(n, total, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big, big + big_cap, st)) !=
-      cudaSuccess)
+  if (up) {
+    for (size_t c = 0; c < up->ready.size(); c++) {
+      if ((e = cudaStreamWaitEvent(st, up->ready[c], 0)) != cudaSuccess) return fail(cuda_fail(e, "upload wait"));
+      if ((e = launch_measure_rows(n, total, up->rows[c], up->rows[c + 1], d_off, d_nbr, d_mask, sel, layout, meas,
+                                   tot, err, big, big + big_cap, st)) != cudaSuccess)
+        return fail(cuda_fail(e, "measure kernel"));
+    }
+  } else if ((e = launch_measure_rows(n, total, 0, n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big,
+                                      big + big_cap, st)) != cudaSuccess) {
     return fail(cuda_fail(e, "measure kernel"));
+  }
+  if ((e = launch_measure_big(n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big, big + big_cap, st)) !=
+      cudaSuccess)
+    return fail(cuda_fail(e, "measure kernel (long rows)"));
   uint32_t herr = 0;
   cudaMemcpyAsync(&m->tot, tot, sizeof(BuildTotals), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -111,9 +172,9 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   if ((e = launch_scan_units(n, meas, off16, tmp, scan_tmp_words(nn), st)) != cudaSuccess)
     return fail(cuda_fail(e, "scan"));
   m->arena_units = m->tot.payload_units;
-  if ((e = cudaMalloc((void**)&m->desc, nn * sizeof(RowDesc))) != cudaSuccess ||
-      (e = cudaMalloc((void**)&m->arena, (m->arena_units + 1) * 16)) != cudaSuccess ||
-      (e = cudaMalloc((void**)&m->counters, 128)) != cudaSuccess)
+  if ((e = pool_alloc((void**)&m->desc, nn * sizeof(RowDesc), st)) != cudaSuccess ||
+      (e = pool_alloc((void**)&m->arena, (m->arena_units + 1) * 16, st)) != cudaSuccess ||
+      (e = pool_alloc((void**)&m->counters, 128, st)) != cudaSuccess)
     return fail(set_error(EH_ERR_OUT_OF_MEMORY, "matrix allocation (%llu bytes) failed: %s",
                           (unsigned long long)((m->arena_units + 1) * 16 + nn * 16), cudaGetErrorString(e)));
   // Words 0..15: work-queue counters; 16..17: the u64 result of the synchronous calls.
@@ -146,9 +207,9 @@ eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaSt
   uint32_t* start = nullptr;
   uint32_t* tmp = nullptr;
   const uint32_t nh = n_heavy ? n_heavy : 1;
-  CU(cudaMallocAsync((void**)&cnt, nh * sizeof(uint32_t), st), "unit scratch");
-  CU(cudaMallocAsync((void**)&start, nh * sizeof(uint32_t), st), "unit scratch");
-  CU(cudaMallocAsync((void**)&tmp, scan_tmp_words(nh) * sizeof(uint32_t), st), "unit scratch");
+  CU(pool_alloc((void**)&cnt, nh * sizeof(uint32_t), st), "unit scratch");
+  CU(pool_alloc((void**)&start, nh * sizeof(uint32_t), st), "unit scratch");
+  CU(pool_alloc((void**)&tmp, scan_tmp_words(nh) * sizeof(uint32_t), st), "unit scratch");
   CU(launch_pivot_units(m->desc, p.order, n_heavy, unit_span, cnt, st), "unit count");
   uint32_t n_units = 0;
   if (n_heavy) {
@@ -166,7 +227,7 @@ eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaSt
       m->device_bytes -= p.units_cap * sizeof(uint2);
     }
     p.units_cap = n_units ? n_units : 1;
-    CU(cudaMalloc((void**)&p.units, p.units_cap * sizeof(uint2)), "unit allocation");
+    CU(pool_alloc((void**)&p.units, p.units_cap * sizeof(uint2), st), "unit allocation");
     m->device_bytes += p.units_cap * sizeof(uint2);
   }
   CU(launch_pivot_unit_fill(cnt, start, n_heavy, p.units, st), "unit fill");
@@ -197,7 +258,7 @@ eh_status ensure_core(Matrix* m, cudaStream_t st) {
   }
   if (want == 0) return EH_OK;
   const uint64_t words = core_row_offset(want);
-  CU(cudaMalloc((void**)&p.core, words * 8), "core allocation");
+  CU(pool_alloc((void**)&p.core, words * 8, st), "core allocation");
   m->device_bytes += words * 8;
   CU(launch_core_build(m->desc, m->arena, want, p.core, st), "core build");
   CU(cudaStreamSynchronize(st), "core build");
@@ -214,10 +275,10 @@ eh_status ensure_plan(Matrix* m, cudaStream_t st) {
     uint32_t* hist = nullptr;
     uint32_t* cursor = nullptr;
     const uint64_t nn = m->n ? m->n : 1;
-    CU(cudaMalloc((void**)&p.order, nn * sizeof(uint32_t)), "plan order allocation");
+    CU(pool_alloc((void**)&p.order, nn * sizeof(uint32_t), st), "plan order allocation");
     m->device_bytes += nn * sizeof(uint32_t);
-    CU(cudaMallocAsync((void**)&hist, (65536 + scan_tmp_words(65536)) * sizeof(uint32_t), st), "plan scratch");
-    CU(cudaMallocAsync((void**)&cursor, 65536 * sizeof(uint32_t), st), "plan scratch");
+    CU(pool_alloc((void**)&hist, (65536 + scan_tmp_words(65536)) * sizeof(uint32_t), st), "plan scratch");
+    CU(pool_alloc((void**)&cursor, 65536 * sizeof(uint32_t), st), "plan scratch");
     CU(launch_plan(m->n, m->desc, 2, hist, p.order, cursor, st), "plan kernels");
     std::vector<uint32_t> starts(65536);
     uint32_t total = 0;
@@ -250,8 +311,8 @@ eh_status ensure_plan(Matrix* m, cudaStream_t st) {
         }
       }
     }
-    CU(cudaMalloc((void**)&p.giant_off, goff.size() * sizeof(unsigned long long)), "giant allocation");
-    CU(cudaMalloc((void**)&p.giant_lists, (gtotal ? gtotal : 1) * sizeof(uint32_t)), "giant allocation");
+    CU(pool_alloc((void**)&p.giant_off, goff.size() * sizeof(unsigned long long), st), "giant allocation");
+    CU(pool_alloc((void**)&p.giant_lists, (gtotal ? gtotal : 1) * sizeof(uint32_t), st), "giant allocation");
     m->device_bytes += goff.size() * 8 + (gtotal ? gtotal : 1) * 4;
     CU(cudaMemcpyAsync(p.giant_off, goff.data(), goff.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
                        st),
@@ -259,8 +320,8 @@ eh_status ensure_plan(Matrix* m, cudaStream_t st) {
     if (!dec_rows.empty()) {
       uint32_t* d_rows = nullptr;
       unsigned long long* d_off = nullptr;
-      CU(cudaMallocAsync((void**)&d_rows, dec_rows.size() * 4, st), "giant scratch");
-      CU(cudaMallocAsync((void**)&d_off, dec_off.size() * 8, st), "giant scratch");
+      CU(pool_alloc((void**)&d_rows, dec_rows.size() * 4, st), "giant scratch");
+      CU(pool_alloc((void**)&d_off, dec_off.size() * 8, st), "giant scratch");
       CU(cudaMemcpyAsync(d_rows, dec_rows.data(), dec_rows.size() * 4, cudaMemcpyHostToDevice, st), "giant copy");
       CU(cudaMemcpyAsync(d_off, dec_off.data(), dec_off.size() * 8, cudaMemcpyHostToDevice, st), "giant copy");
       CU(launch_decode_rows(m->desc, m->arena, d_rows, d_off, (uint32_t)dec_rows.size(), p.giant_lists, st),
@@ -439,26 +500,82 @@ eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* n
   EH_CHECK_ARG(sel != EH_SELECT_MASK || edge_mask != nullptr || m == 0, "EH_SELECT_MASK needs an edge mask");
   // Offsets are checked on the device (each row must lie within [0, offsets[n])).
   cudaStream_t st = ST(stream);
+  cudaStream_t cs = nullptr;
   uint64_t* d_off = nullptr;
   uint32_t* d_nbr = nullptr;
   uint8_t* d_mask = nullptr;
   cudaError_t e;
-  if ((e = cudaMallocAsync((void**)&d_off, (n + 1) * 8, st)) != cudaSuccess ||
-      (e = cudaMallocAsync((void**)&d_nbr, (m ? m : 1) * 4, st)) != cudaSuccess ||
-      (sel == EH_SELECT_MASK && (e = cudaMallocAsync((void**)&d_mask, m ? m : 1, st)) != cudaSuccess)) {
+  if ((e = eh::upload_stream(&cs)) != cudaSuccess) return eh::cuda_fail(e, "upload stream");
+  if ((e = eh::pool_alloc((void**)&d_off, (n + 1) * 8, st)) != cudaSuccess ||
+      (e = eh::pool_alloc((void**)&d_nbr, (m ? m : 1) * 4, st)) != cudaSuccess ||
+      (sel == EH_SELECT_MASK && (e = eh::pool_alloc((void**)&d_mask, m ? m : 1, st)) != cudaSuccess)) {
     cudaFreeAsync(d_off, st);
     cudaFreeAsync(d_nbr, st);
     return set_error(EH_ERR_OUT_OF_MEMORY, "input upload allocation failed: %s", cudaGetErrorString(e));
   }
-  cudaMemcpyAsync(d_off, offsets, (n + 1) * 8, cudaMemcpyHostToDevice, st);
-  if (m) cudaMemcpyAsync(d_nbr, nbrs, m * 4, cudaMemcpyHostToDevice, st);
-  if (d_mask && m) cudaMemcpyAsync(d_mask, edge_mask, m, cudaMemcpyHostToDevice, st);
+  // The adjacency goes up in chunks of rows (about kUploadChunkEntries entries
+  // each) on the upload stream, and the build's first pass measures each chunk
+  // as soon as it has landed, so the copy over the host link and the measure
+  // pass overlap.  Chunk boundaries come from a binary search of the host
+  // offsets; the byte ranges are clamped to stay monotone within [0, m) so
+  // that every entry is copied exactly once whatever the offsets hold (rows
+  // with bad offsets are rejected by the measure pass).
+  constexpr uint64_t kUploadChunkEntries = 16ull << 20;
+  constexpr uint64_t kUploadMaxChunks = 16;
+  const uint64_t chunks =
+      std::max<uint64_t>(1, std::min<uint64_t>(kUploadMaxChunks, (m + kUploadChunkEntries - 1) / kUploadChunkEntries));
+  eh::UploadChunks up;
+  up.rows.push_back(0);
+  for (uint64_t c = 1; c < chunks; c++) {
+    const uint64_t target = m / chunks * c;
+    uint64_t lo = 0, hi = n;  // first row whose offset reaches target
+    while (lo < hi) {
+      const uint64_t mid = lo + (hi - lo) / 2;
+      if (offsets[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    up.rows.push_back(std::max(lo, up.rows.back()));
+  }
+  up.rows.push_back(n);
+  eh_status s = EH_OK;
+  cudaEvent_t allocated = nullptr;
+  auto event = [](cudaEvent_t* ev) { return cudaEventCreateWithFlags(ev, cudaEventDisableTiming); };
+  if ((e = event(&allocated)) != cudaSuccess || (e = cudaEventRecord(allocated, st)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(cs, allocated, 0)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(d_off, offsets, (n + 1) * 8, cudaMemcpyHostToDevice, cs)) != cudaSuccess)
+    s = eh::cuda_fail(e, "upload");
+  uint64_t copied = 0;
+  for (uint64_t c = 0; c < chunks && s == EH_OK; c++) {
+    const uint64_t upto = c + 1 == chunks ? m : std::min(m, std::max(copied, offsets[up.rows[c + 1]]));
+    if (upto > copied) {
+      if ((e = cudaMemcpyAsync(d_nbr + copied, nbrs + copied, (upto - copied) * 4, cudaMemcpyHostToDevice, cs)) !=
+              cudaSuccess ||
+          (d_mask && (e = cudaMemcpyAsync(d_mask + copied, edge_mask + copied, upto - copied, cudaMemcpyHostToDevice,
+                                          cs)) != cudaSuccess)) {
+        s = eh::cuda_fail(e, "upload");
+        break;
+      }
+    }
+    copied = upto;
+    cudaEvent_t ev = nullptr;
+    if ((e = event(&ev)) != cudaSuccess) {
+      s = eh::cuda_fail(e, "upload event");
+      break;
+    }
+    up.ready.push_back(ev);
+    if ((e = cudaEventRecord(ev, cs)) != cudaSuccess) s = eh::cuda_fail(e, "upload event");
+  }
   Matrix* mx = nullptr;
-  eh_status s = eh::build_device(n, d_off, d_nbr, d_mask, (int)sel, (int)layout, st, &mx, m);
+  if (s == EH_OK) s = eh::build_device(n, d_off, d_nbr, d_mask, (int)sel, (int)layout, st, &mx, m, &up);
   if (s == EH_OK) *out = reinterpret_cast<eh_matrix_t>(mx);
+  // Every copy has landed before the upload buffers go back to the pool.
+  if (!up.ready.empty()) cudaStreamWaitEvent(st, up.ready.back(), 0);
+  else if (allocated) cudaStreamSynchronize(cs);
   cudaFreeAsync(d_off, st);
   cudaFreeAsync(d_nbr, st);
   if (d_mask) cudaFreeAsync(d_mask, st);
+  if (allocated) cudaEventDestroy(allocated);
+  for (cudaEvent_t ev : up.ready) cudaEventDestroy(ev);
   return s;
 }
 

@@ -36,11 +36,17 @@ struct BuildTotals {  // accumulated with atomics by the measure pass
 };
 
 // eh_build.cu
-// big / n_big: the rows longer than 4,096 entries (measured and encoded by
-// whole CTAs), at most big_row_capacity(n, total) of them.
-cudaError_t launch_measure(uint64_t n, uint64_t total, const uint64_t* off, const uint32_t* nbr,
-                           const uint8_t* mask, int sel, int layout, RowMeasure* meas, BuildTotals* totals,
-                           uint32_t* err, uint32_t* big, uint32_t* n_big, cudaStream_t st);
+// Pass 1 over rows [r_begin, r_end) of an n-row matrix (a launch per uploaded
+// chunk of rows, or one for all): rows up to 4,096 entries are measured by a
+// warp each; longer rows are appended to big / n_big (at most
+// big_row_capacity(n, total) of them) for launch_measure_big, which runs once
+// after every row range and measures them by whole CTAs.
+cudaError_t launch_measure_rows(uint64_t n, uint64_t total, uint64_t r_begin, uint64_t r_end, const uint64_t* off,
+                                const uint32_t* nbr, const uint8_t* mask, int sel, int layout, RowMeasure* meas,
+                                BuildTotals* totals, uint32_t* err, uint32_t* big, uint32_t* n_big, cudaStream_t st);
+cudaError_t launch_measure_big(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask, int sel,
+                               int layout, RowMeasure* meas, BuildTotals* totals, uint32_t* err, const uint32_t* big,
+                               const uint32_t* n_big, cudaStream_t st);
 uint64_t big_row_capacity(uint64_t n, uint64_t total);
 cudaError_t launch_scan_units(uint64_t n, const RowMeasure* meas, uint32_t* off16, uint32_t* block_tmp,
                               uint64_t n_block_tmp, cudaStream_t st);

@@ -70,11 +70,33 @@ struct Matrix {
 };
 
 // eh_capi.cu
+// Stream-ordered allocation (cudaMallocAsync semantics) from the library's own
+// pool on the current device, for scratch (freed with cudaFreeAsync) and for a
+// matrix's buffers (freed with cudaFree, which waits for the device; every
+// build and plan step synchronises its stream before other streams use them).
+// The pool keeps up to kPoolKeep bytes of freed memory mapped between calls:
+// the device's default pool releases it at every synchronisation, and mapping
+// 400 MB again costs about 1 ms on GB300.
+constexpr uint64_t kPoolKeep = 4ull << 30;
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st);
+// A non-blocking stream of the current device for host uploads that overlap
+// the build (one per device, created on first use).
+cudaError_t upload_stream(cudaStream_t* out);
+
+// A host upload in flight: rows [rows[c], rows[c + 1]) of the adjacency have
+// landed on the device once ready[c] has completed.
+struct UploadChunks {
+  std::vector<uint64_t> rows;
+  std::vector<cudaEvent_t> ready;
+};
+
 // total = offsets[n] (the neighbour array's length), or kTotalUnknown to read it
-// from the device.
+// from the device.  With `up`, the first pass measures each chunk of rows as
+// soon as its upload has landed (the offsets must be in place before chunk 0's
+// event); without, the whole input is already on the device.
 constexpr uint64_t kTotalUnknown = ~0ull;
 eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask, int sel,
-                       int layout, cudaStream_t st, Matrix** out, uint64_t total);
+                       int layout, cudaStream_t st, Matrix** out, uint64_t total, const UploadChunks* up = nullptr);
 eh_status ensure_plan(Matrix* m, cudaStream_t st);
 eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaStream_t st);
 eh_status ensure_core(Matrix* m, cudaStream_t st);

@@ -363,7 +363,7 @@ extern "C" eh_status eh_symbiosity_async(eh_matrix_t rh, eh_matrix_t ch, double 
   if (r->n == 0) return EH_OK;
   // Heavy-row list: n entries, then its length, the CTAs' cursor and the warps' cursor.
   uint32_t* scratch = nullptr;
-  e = cudaMallocAsync((void**)&scratch, (r->n + 3) * sizeof(uint32_t), st);
+  e = pool_alloc((void**)&scratch, (r->n + 3) * sizeof(uint32_t), st);
   if (e != cudaSuccess) return set_error(EH_ERR_OUT_OF_MEMORY, "symbiosity scratch: %s", cudaGetErrorString(e));
   uint32_t* counts = scratch + r->n;
   e = cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st);
@@ -415,7 +415,7 @@ extern "C" eh_status eh_bfs_path_length(eh_matrix_t mh, uint32_t start, uint64_t
   const uint64_t words = (n + 64) / 64;
   const size_t bytes = 2 * words * 8 + 2 * n * 4 + (kBfsChunk + 1) * sizeof(LevelCount) + 8;
   char* base = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&base, bytes, st);
+  cudaError_t e = pool_alloc((void**)&base, bytes, st);
   if (e != cudaSuccess) return set_error(EH_ERR_OUT_OF_MEMORY, "BFS scratch (%zu bytes): %s", bytes, cudaGetErrorString(e));
   BfsArgs a;
   a.desc = m->desc;
