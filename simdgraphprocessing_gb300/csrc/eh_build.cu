@@ -229,14 +229,15 @@ __global__ void __launch_bounds__(kBigBlock) k_measure_big(uint64_t n, const uin
                                                            RowMeasure* __restrict__ meas,
                                                            BuildTotals* __restrict__ tot, uint32_t* __restrict__ err,
                                                            const uint32_t* __restrict__ big,
-                                                           const uint32_t* __restrict__ n_big) {
+                                                           const uint32_t* __restrict__ big_begin,
+                                                           const uint32_t* __restrict__ big_end) {
   constexpr int NWB = kBigBlock / 32;
   __shared__ SegMeasure s_seg[NWB];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t nb = *n_big;
+  const uint32_t nb = *big_end;
   Totals t;
   uint32_t flags = 0;
-  for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
+  for (uint32_t i = *big_begin + blockIdx.x; i < nb; i += gridDim.x) {
     const uint64_t row = big[i];
     const uint64_t b = off[row], e = off[row + 1];
     const uint64_t slice = ((e - b + NWB - 1) / NWB + 31) & ~31ull;
@@ -641,9 +642,10 @@ cudaError_t launch_measure_rows(uint64_t n, uint64_t total, uint64_t r_begin, ui
 
 cudaError_t launch_measure_big(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask, int sel,
                                int layout, RowMeasure* meas, BuildTotals* totals, uint32_t* err, const uint32_t* big,
-                               const uint32_t* n_big, cudaStream_t st) {
+                               const uint32_t* big_begin, const uint32_t* big_end, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_measure_big<<<2 * 152, kBigBlock, 0, st>>>(n, off, nbr, mask, sel, layout, meas, totals, err, big, n_big);
+  k_measure_big<<<2 * 152, kBigBlock, 0, st>>>(n, off, nbr, mask, sel, layout, meas, totals, err, big, big_begin,
+                                               big_end);
   return cudaGetLastError();
 }
 

@@ -110,8 +110,12 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   uint32_t* err = nullptr;
   uint32_t* off16 = nullptr;
   uint32_t* tmp = nullptr;
-  uint32_t* big = nullptr;  // rows over 4,096 entries, then their count
+  // big: rows over 4,096 entries (big_cap slots), their count n_big, then
+  // n_big as it stood after each uploaded chunk of rows (mark[0] = 0), so that
+  // each chunk's long rows are measured right after it.
+  uint32_t* big = nullptr;
   const uint64_t big_cap = big_row_capacity(n, total);
+  const uint64_t n_marks = (up ? up->ready.size() : 0) + 1;
   auto cleanup = [&]() {
     cudaFreeAsync(meas, st);
     cudaFreeAsync(tot, st);
@@ -136,26 +140,30 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
       (e = pool_alloc((void**)&err, sizeof(uint32_t), st)) != cudaSuccess ||
       (e = pool_alloc((void**)&off16, nn * sizeof(uint32_t), st)) != cudaSuccess ||
       (e = pool_alloc((void**)&tmp, scan_tmp_words(nn) * sizeof(uint32_t), st)) != cudaSuccess ||
-      (e = pool_alloc((void**)&big, (big_cap + 1) * sizeof(uint32_t), st)) != cudaSuccess)
+      (e = pool_alloc((void**)&big, (big_cap + 1 + n_marks) * sizeof(uint32_t), st)) != cudaSuccess)
     return fail(e == cudaErrorMemoryAllocation ? set_error(EH_ERR_OUT_OF_MEMORY, "build scratch allocation failed")
                                                : cuda_fail(e, "cudaMallocAsync"));
   cudaMemsetAsync(tot, 0, sizeof(BuildTotals), st);
   cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
-  cudaMemsetAsync(big + big_cap, 0, sizeof(uint32_t), st);
+  uint32_t* n_big = big + big_cap;
+  uint32_t* mark = n_big + 1;
+  cudaMemsetAsync(n_big, 0, 2 * sizeof(uint32_t), st);  // n_big, mark[0]
   if (up) {
     for (size_t c = 0; c < up->ready.size(); c++) {
       if ((e = cudaStreamWaitEvent(st, up->ready[c], 0)) != cudaSuccess) return fail(cuda_fail(e, "upload wait"));
       if ((e = launch_measure_rows(n, total, up->rows[c], up->rows[c + 1], d_off, d_nbr, d_mask, sel, layout, meas,
-                                   tot, err, big, big + big_cap, st)) != cudaSuccess)
+                                   tot, err, big, n_big, st)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(mark + c + 1, n_big, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st)) != cudaSuccess ||
+          (e = launch_measure_big(n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big, mark + c, mark + c + 1,
+                                  st)) != cudaSuccess)
         return fail(cuda_fail(e, "measure kernel"));
     }
-  } else if ((e = launch_measure_rows(n, total, 0, n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big,
-                                      big + big_cap, st)) != cudaSuccess) {
+  } else if ((e = launch_measure_rows(n, total, 0, n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big, n_big,
+                                      st)) != cudaSuccess ||
+             (e = launch_measure_big(n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big, mark, n_big, st)) !=
+                 cudaSuccess) {
     return fail(cuda_fail(e, "measure kernel"));
   }
-  if ((e = launch_measure_big(n, d_off, d_nbr, d_mask, sel, layout, meas, tot, err, big, big + big_cap, st)) !=
-      cudaSuccess)
-    return fail(cuda_fail(e, "measure kernel (long rows)"));
   uint32_t herr = 0;
   cudaMemcpyAsync(&m->tot, tot, sizeof(BuildTotals), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);

@@ -39,14 +39,15 @@ struct BuildTotals {  // accumulated with atomics by the measure pass
 // Pass 1 over rows [r_begin, r_end) of an n-row matrix (a launch per uploaded
 // chunk of rows, or one for all): rows up to 4,096 entries are measured by a
 // warp each; longer rows are appended to big / n_big (at most
-// big_row_capacity(n, total) of them) for launch_measure_big, which runs once
-// after every row range and measures them by whole CTAs.
+// big_row_capacity(n, total) of them).  launch_measure_big measures the list
+// entries [*big_begin, *big_end) by whole CTAs (device words, read when the
+// kernel runs: the rows a range appended, or all of them).
 cudaError_t launch_measure_rows(uint64_t n, uint64_t total, uint64_t r_begin, uint64_t r_end, const uint64_t* off,
                                 const uint32_t* nbr, const uint8_t* mask, int sel, int layout, RowMeasure* meas,
                                 BuildTotals* totals, uint32_t* err, uint32_t* big, uint32_t* n_big, cudaStream_t st);
 cudaError_t launch_measure_big(uint64_t n, const uint64_t* off, const uint32_t* nbr, const uint8_t* mask, int sel,
                                int layout, RowMeasure* meas, BuildTotals* totals, uint32_t* err, const uint32_t* big,
-                               const uint32_t* n_big, cudaStream_t st);
+                               const uint32_t* big_begin, const uint32_t* big_end, cudaStream_t st);
 uint64_t big_row_capacity(uint64_t n, uint64_t total);
 cudaError_t launch_scan_units(uint64_t n, const RowMeasure* meas, uint32_t* off16, uint32_t* block_tmp,
                               uint64_t n_block_tmp, cudaStream_t st);
