@@ -127,6 +127,36 @@ def test_rejects_bad_offsets_without_fault(eh):
     assert m.count_triangles() == 1
 
 
+def test_chunked_host_upload_equals_device_build(eh):
+    """A build from host arrays uploads the adjacency in chunks of rows (about
+    16 M entries each) and measures each chunk as it lands.  At about 42 M
+    entries (three chunks, the long rows in the first) it must encode byte for
+    byte as the single-pass build from device buffers, and falling offsets in a
+    later chunk must still be rejected."""
+    import hashlib
+    import torch
+    g = eh.graph("rmat", 21, scale=21, edges=21 << 20)
+    off, nbr = g.csr()[:2]
+    assert int(off[-1]) > 2 * (16 << 20)
+    d_off = torch.from_numpy(off.view(np.int64)).cuda()
+    d_nbr = torch.from_numpy(nbr.view(np.int32)).cuda()
+    for layout in ("hybrid", "pshort"):
+        a = eh.Matrix.build(off, nbr, selection="lower", layout=layout)
+        b = eh.Matrix.build_device(len(off) - 1, d_off.data_ptr(), d_nbr.data_ptr(), selection="lower",
+                                   layout=layout)
+        assert a.info() == b.info()
+        assert hashlib.sha256(a.export_flattened()).digest() == hashlib.sha256(b.export_flattened()).digest()
+        assert a.count_triangles() == b.count_triangles()
+        del a, b
+    bad = off.copy()
+    k = int(np.searchsorted(off, off[-1] * 3 // 4))  # a row in the last chunk
+    assert off[k + 1] < off[-1]
+    bad[k] = bad[k + 1] + 1  # row k falls; row k - 1 stays within the neighbour array
+    with pytest.raises(eh.EHError) as ei:
+        eh.Matrix.build(bad, nbr, selection="lower", layout="hybrid")
+    assert "offsets" in str(ei.value)
+
+
 def test_empty_and_tiny_graphs(eh, oracle):
     for off, nbr in [(np.zeros(1, np.uint64), np.zeros(0, np.uint32)),
                      (np.zeros(5, np.uint64), np.zeros(0, np.uint32)),
