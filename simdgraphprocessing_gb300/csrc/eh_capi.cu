@@ -229,8 +229,8 @@ eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaSt
     n_units = last_start + last_cnt;
   }
   if (!p.units || p.units_cap < (uint64_t)n_units) {
-    CU(cudaStreamSynchronize(st), "units");
     if (p.units) {
+      CU(cudaDeviceSynchronize(), "units");  // launches on other streams may still read them
       cudaFree(p.units);
       m->device_bytes -= p.units_cap * sizeof(uint2);
     }
@@ -258,7 +258,7 @@ eh_status ensure_core(Matrix* m, cudaStream_t st) {
   if (m->n < 4096) want = 0;
   if (want == p.core_k && (want == 0 || p.core)) return EH_OK;
   if (p.core) {
-    CU(cudaStreamSynchronize(st), "core");
+    CU(cudaDeviceSynchronize(), "core");  // launches on other streams may still read it
     cudaFree(p.core);
     m->device_bytes -= core_row_offset(p.core_k) * 8;
     p.core = nullptr;
@@ -714,6 +714,9 @@ void eh_matrix_free(eh_matrix_t mh) {
   Matrix* m = MX(mh);
   if (!m) return;
   cudaSetDevice(m->device);
+  // cudaFree does not wait for the device on stream-ordered (pool) memory:
+  // let every launch that may still read the matrix finish first.
+  cudaDeviceSynchronize();
   cudaFree(m->desc);
   cudaFree(m->arena);
   cudaFree(m->counters);

@@ -72,8 +72,9 @@ struct Matrix {
 // eh_capi.cu
 // Stream-ordered allocation (cudaMallocAsync semantics) from the library's own
 // pool on the current device, for scratch (freed with cudaFreeAsync) and for a
-// matrix's buffers (freed with cudaFree, which waits for the device; every
-// build and plan step synchronises its stream before other streams use them).
+// matrix's buffers (freed with cudaFree after cudaDeviceSynchronize: cudaFree
+// does not wait for the device on pool memory; every build and plan step
+// synchronises its stream before other streams use them).
 // The pool keeps up to kPoolKeep bytes of freed memory mapped between calls:
 // the device's default pool releases it at every synchronisation, and mapping
 // 400 MB again costs about 1 ms on GB300.
