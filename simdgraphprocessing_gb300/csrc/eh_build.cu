@@ -31,6 +31,11 @@ __device__ __forceinline__ bool is_selected(int sel, uint32_t x, uint64_t row, c
 // after the rest of the grid has finished.
 constexpr uint64_t kBigRow = 4096;
 constexpr int kBigBlock = 1024;
+// Rows up to this many entries are measured and encoded by one lane each (most
+// rows of a power-law graph: at R-MAT scale 22, 77% of the rows and 3% of the
+// entries), so that a warp does not spend a round of shuffles and ballots on
+// each of them.
+constexpr uint64_t kLaneRow = 8;
 
 struct SegMeasure {
   uint32_t cnt, parts, first, last, first_hi, last_hi, flags;
@@ -159,6 +164,19 @@ struct Totals {
     max_full = max(max_full, (unsigned long long)full);
     max_card = max(max_card, (unsigned long long)r.m.card);
   }
+  // Sums / maxima over the warp, left in every lane.
+  __device__ __forceinline__ void warp_reduce() {
+    card = warp_sum_u64(card);
+    ref = warp_sum_u64(ref);
+    units = warp_sum_u64(units);
+    for (int d = 16; d; d >>= 1) {
+      max_full = max(max_full, __shfl_xor_sync(FULL, max_full, d));
+      max_card = max(max_card, __shfl_xor_sync(FULL, max_card, d));
+    }
+    n_uint = __reduce_add_sync(FULL, n_uint);
+    n_pshort = __reduce_add_sync(FULL, n_pshort);
+    n_bitset = __reduce_add_sync(FULL, n_bitset);
+  }
   __device__ __forceinline__ void flush(BuildTotals* tot) const {
     if (card) atomicAdd(&tot->cardinality, card);
     if (ref) atomicAdd(&tot->ref_bytes, ref);
@@ -182,23 +200,44 @@ __global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, uint64_t total, 
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
   uint32_t flags = 0;
-  Totals t;  // lane 0's running totals for this warp's rows (one atomic each at the end)
+  Totals t;  // this lane's running totals (summed over the warp, one atomic each at the end)
   // Rows [r_begin, r_end) are dealt to warps round-robin (row = r_begin + warp
   // + i * warps, so that the degree-ordered hubs at the front spread over the
   // grid); a warp loads the offsets of its next 32 rows at once (lane q: its
-  // q-th row), then measures them one by one.
+  // q-th row).  Each lane measures its own row if it has at most kLaneRow
+  // entries; the warp then measures the longer ones one by one.
   for (uint64_t row0 = r_begin + (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row0 < r_end;
        row0 += nw * 32) {
     const uint64_t my = row0 + lane * nw;
-    const uint64_t my_b = my < r_end ? off[my] : 0, my_e = my < r_end ? off[my + 1] : 0;
-    for (uint32_t q = 0; q < 32; q++) {
-      const uint64_t row = row0 + q * nw;
-      if (row >= r_end) break;
-      uint64_t b = __shfl_sync(FULL, my_b, q), e = __shfl_sync(FULL, my_e, q);
-      if (e < b || e > total) {  // offsets must rise monotonically within the nbr array
-        flags |= ERRF_OFFSETS;
-        b = e = 0;
+    uint64_t my_b = my < r_end ? off[my] : 0, my_e = my < r_end ? off[my + 1] : 0;
+    if (my_e < my_b || my_e > total) {  // offsets must rise monotonically within the nbr array
+      flags |= ERRF_OFFSETS;
+      my_b = my_e = 0;
+    }
+    const bool lane_row = my < r_end && my_e - my_b <= kLaneRow;
+    if (lane_row) {
+      uint32_t cnt = 0, parts = 0, first = 0xffffffffu, last = 0, prev = 0, prev_hi = 0;
+      for (uint64_t k = my_b; k < my_e; k++) {
+        const uint32_t x = nbr[k];
+        if (x >= n) flags |= ERRF_RANGE;
+        if (k > my_b && prev >= x) flags |= ERRF_UNSORTED;
+        prev = x;
+        if (is_selected(sel, x, my, mask, k)) {
+          if (cnt == 0 || (x >> 16) != prev_hi) parts++;  // a new 16-bit partition
+          prev_hi = x >> 16;
+          first = min(first, x);
+          last = max(last, x);
+          cnt++;
+        }
       }
+      const RowResult r = finish_row(cnt, parts, first, last, layout);
+      meas[my] = r.m;
+      t.add(r, my_e - my_b);
+    }
+    for (uint32_t rest = __ballot_sync(FULL, my < r_end && !lane_row); rest; rest &= rest - 1) {
+      const uint32_t q = __ffs(rest) - 1;
+      const uint64_t row = row0 + q * nw;
+      const uint64_t b = __shfl_sync(FULL, my_b, q), e = __shfl_sync(FULL, my_e, q);
       if (e - b > kBigRow) {
         if (lane == 0) big[atomicAdd(n_big, 1u)] = (uint32_t)row;
         continue;
@@ -213,6 +252,8 @@ __global__ void __launch_bounds__(kBlock) k_measure(uint64_t n, uint64_t total, 
       }
     }
   }
+  t.warp_reduce();
+  flags = __reduce_or_sync(FULL, flags);
   if (lane == 0) {
     t.flush(tot);
     if (flags) atomicOr(err, flags);
@@ -407,8 +448,9 @@ __global__ void __launch_bounds__(kBlock) k_encode(uint64_t n, const uint64_t* _
   const uint64_t nw = (uint64_t)gridDim.x * (kBlock / 32);
   // Rows are dealt to warps round-robin as in k_measure; lane q loads the measure,
   // offsets and payload start of the warp's q-th next row and writes its
-  // RowDesc, then the warp writes the payloads one row after another (rows
-  // longer than kBigRow are left to k_encode_big).
+  // RowDesc and, for rows of at most kLaneRow entries, its payload; the warp
+  // then writes the longer rows' payloads one row after another (rows longer
+  // than kBigRow are left to k_encode_big).
   for (uint64_t row0 = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); row0 < n; row0 += nw * 32) {
     const uint64_t my = row0 + lane * nw;
     RowMeasure mm{0, 0, 0, 0};
@@ -421,14 +463,33 @@ __global__ void __launch_bounds__(kBlock) k_encode(uint64_t n, const uint64_t* _
       my_e = off[my + 1];
       desc[my] = RowDesc{my_o, mm.card, mm.aux, mm.lt};
     }
-    for (uint32_t q = 0; q < 32; q++) {
+    const bool lane_row = my < n && my_e - my_b <= kLaneRow;
+    if (lane_row && mm.card) {  // the lane owns the row's payload units
+      uint4* dst = arena + my_o;
+      const uint32_t type = mm.lt >> 30;
+      if (type == TY_PSHORT) {
+        write_pshort(reinterpret_cast<uint16_t*>(dst), my, my_b, my_e, nbr, mask, sel);
+      } else if (type == TY_UINT) {
+        uint32_t* a = reinterpret_cast<uint32_t*>(dst);
+        for (uint64_t k = my_b; k < my_e; k++) {
+          const uint32_t x = nbr[k];
+          if (is_selected(sel, x, my, mask, k)) *a++ = x;
+        }
+      } else {
+        unsigned long long* words = reinterpret_cast<unsigned long long*>(dst);
+        for (uint64_t k = my_b; k < my_e; k++) {
+          const uint32_t x = nbr[k];
+          if (is_selected(sel, x, my, mask, k)) words[(x >> 6) - mm.aux] |= 1ull << (x & 63);
+        }
+      }
+    }
+    for (uint32_t rest = __ballot_sync(FULL, my < n && !lane_row && mm.card != 0); rest; rest &= rest - 1) {
+      const uint32_t q = __ffs(rest) - 1;
       const uint64_t row = row0 + q * nw;
-      if (row >= n) break;
-      const uint32_t card = __shfl_sync(FULL, mm.card, q);
       const uint32_t aux = __shfl_sync(FULL, mm.aux, q);
       const uint32_t type = __shfl_sync(FULL, mm.lt, q) >> 30;
       const uint64_t b = __shfl_sync(FULL, my_b, q), e = __shfl_sync(FULL, my_e, q);
-      if (card == 0 || e - b > kBigRow) continue;
+      if (e - b > kBigRow) continue;
       uint4* dst = arena + __shfl_sync(FULL, my_o, q);
       if (type == TY_PSHORT) {
         if (lane == 0) write_pshort(reinterpret_cast<uint16_t*>(dst), row, b, e, nbr, mask, sel);
