@@ -166,9 +166,12 @@ typedef struct eh_matrix_info {
 
 /* SparseMatrix<T,R>::build -> from_symmetric_noattribute_graph
  * (src/SparseMatrix.hpp:268-290,406-494) and pack_data (:249-266).
- * Host pointers; the adjacency is copied to the device, then selected,
- * layout-optimized and encoded there.  `edge_mask` (u8 per entry of nbrs) is
- * read only for EH_SELECT_MASK and may be NULL otherwise. */
+ * Host pointers; the adjacency is copied to the device in chunks of rows on an
+ * internal upload stream, and selected, layout-optimized and encoded there,
+ * each chunk's first pass starting on `stream` as soon as it has landed (the
+ * copy overlaps the build when the host buffers are pinned).  `edge_mask` (u8
+ * per entry of nbrs) is read only for EH_SELECT_MASK and may be NULL
+ * otherwise. */
 eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* nbrs,
                           const uint8_t* edge_mask, eh_selection sel, eh_layout layout,
                           void* stream, eh_matrix_t* out);
@@ -195,6 +198,8 @@ eh_status eh_matrix_get_max_row_id(eh_matrix_t m, uint32_t* row);
 /* Algorithmic bytes of one triangle-count pass:
  * sum_i [8 + bytes(A_i)] + sum_{(i,j) selected} bytes(B_j), bytes = layout payload. */
 eh_status eh_matrix_triangle_bytes(eh_matrix_t m, uint64_t* bytes);
+/* Waits for the device, then returns the matrix's memory to the library's
+ * pool (which keeps up to 4 GiB of freed memory mapped per device). */
 void eh_matrix_free(eh_matrix_t m);
 
 /* ------------------------------------------------------------------------- */
