@@ -30,6 +30,7 @@ import sys
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e nominal; the roofline's `peak` is the measured copy bandwidth
 sys.path.insert(0, ROOT)
 
 L2_FLUSH_BYTES = 256 << 20
@@ -62,6 +63,27 @@ def parse_args():
     p.add_argument("--rate", type=float, default=0.0, help="serve: arrivals per second (0 = 0.8 x measured capacity)")
     p.add_argument("--slots", type=int, default=8, help="serve: concurrent queries on the device")
     return p.parse_args()
+
+
+def cpu_model():
+    """The host CPU as /proc/cpuinfo names it (x86: model name; Arm: implementer / part)."""
+    import platform
+    fields = {}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                fields.setdefault(k.strip(), v.strip())
+    except OSError:
+        pass
+    if "model name" in fields:
+        return fields["model name"]
+    part = fields.get("CPU part")
+    names = {"0xd4f": "Neoverse V2 (Grace)", "0xd40": "Neoverse V1", "0xd0c": "Neoverse N1"}
+    if part:
+        return "%s %s (implementer %s, part %s)" % (platform.machine(), names.get(part, "Arm core"),
+                                                     fields.get("CPU implementer", "?"), part)
+    return platform.machine()
 
 
 def edge_count(a):
@@ -230,6 +252,7 @@ def run_reference(a, rank, world):
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (seeded R-MAT generator)", "config": work,
         "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "cpu": cpu_model(),
                          "sample": sample + "; C oracle port of the reference algorithm (OpenMP)"},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "pruned_edges_total": total_edges,
@@ -339,7 +362,8 @@ def run_ours(a, rank, world, local_rank):
     cpu = None
     if not a.no_cpu and not a.profile and world == 1:
         v, dt, threads, sample, ccount, tb = cpu_count(off, nbr, a.layout)
-        cpu = {"value": v, "unit": "edges/s", "cores": threads, "kind": "port", "sample": sample +
+        cpu = {"value": v, "unit": "edges/s", "cores": threads, "kind": "port", "cpu": cpu_model(),
+               "sample": sample +
                "; C oracle port of the reference algorithm (OpenMP, build %.2f s untimed)" % tb,
                "count_matches_gpu": (ccount == count) if ccount is not None else None}
     res = {
@@ -353,6 +377,7 @@ def run_ours(a, rank, world, local_rank):
                        parallelism="replicas" if world > 1 else "single GPU", work_shape=shape),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "nominal_gbs": NOMINAL_HBM_GBS, "frac_of_nominal": achieved / NOMINAL_HBM_GBS,
                      "algorithmic_bytes_per_launch": btc,
                      "formula": "sum_i [8 + bytes(A_i)] + sum_{(i,j) in E<} bytes(B_j), bytes = layout payload",
                      "dram_gbs": (traffic / (ms / 1e3) / 1e9) if traffic else None,
