@@ -548,7 +548,8 @@ eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* n
   eh_status s = EH_OK;
   cudaEvent_t allocated = nullptr;
   auto event = [](cudaEvent_t* ev) { return cudaEventCreateWithFlags(ev, cudaEventDisableTiming); };
-  if ((e = event(&allocated)) != cudaSuccess || (e = cudaEventRecord(allocated, st)) != cudaSuccess ||
+  if ((e = event(&allocated)) != cudaSuccess) allocated = nullptr;
+  if (e != cudaSuccess || (e = cudaEventRecord(allocated, st)) != cudaSuccess ||
       (e = cudaStreamWaitEvent(cs, allocated, 0)) != cudaSuccess ||
       (e = cudaMemcpyAsync(d_off, offsets, (n + 1) * 8, cudaMemcpyHostToDevice, cs)) != cudaSuccess)
     s = eh::cuda_fail(e, "upload");
@@ -576,9 +577,9 @@ eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* n
   Matrix* mx = nullptr;
   if (s == EH_OK) s = eh::build_device(n, d_off, d_nbr, d_mask, (int)sel, (int)layout, st, &mx, m, &up);
   if (s == EH_OK) *out = reinterpret_cast<eh_matrix_t>(mx);
-  // Every copy has landed before the upload buffers go back to the pool.
-  if (!up.ready.empty()) cudaStreamWaitEvent(st, up.ready.back(), 0);
-  else if (allocated) cudaStreamSynchronize(cs);
+  // Every copy has landed before the upload buffers go back to the pool (after
+  // a successful build the stream has already waited for all of them).
+  if (allocated) cudaStreamSynchronize(cs);
   cudaFreeAsync(d_off, st);
   cudaFreeAsync(d_nbr, st);
   if (d_mask) cudaFreeAsync(d_mask, st);
