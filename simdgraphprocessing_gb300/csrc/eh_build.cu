@@ -3,12 +3,14 @@
 // pack_data (:249-266), the layout optimizer hybrid::get_type
 // (src/set/layouts/hybrid.hpp:73-100) and the encoders T::build_flattened.
 //
-// Pass 1 (k_measure, one warp per row): validate the row (offsets rising within
-// the neighbour array, strictly ascending, ids < n), apply the edge selection,
-// and measure what the layout needs
-// (count, first, last, 16-bit partitions).  Choose the layout and payload size.
+// Pass 1 (k_measure: one lane per row of up to 8 entries, one warp per longer
+// row, one CTA per row over 4,096 entries in k_measure_big): validate the row
+// (offsets rising within the neighbour array, strictly ascending, ids < n),
+// apply the edge selection, and measure what the layout needs (count, first,
+// last, 16-bit partitions).  Choose the layout and payload size.
 // Pass 2: exclusive scan of payload sizes (16-byte units) -> row offsets.
-// Pass 3 (k_encode, one warp per row): write RowDesc and the payload.
+// Pass 3 (k_encode / k_encode_big, the same split): write RowDesc and the
+// payload.
 #include <algorithm>
 #include <cstdint>
 
