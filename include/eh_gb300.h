@@ -321,7 +321,9 @@ void eh_batch_free(eh_batch_t b);
 typedef struct eh_server* eh_server_t;
 typedef struct eh_server_config {
   uint32_t slots;          /* concurrent queries on the device (1..64)            */
-  uint64_t hbm_cap_bytes;  /* resident matrices + query scratch never exceed this */
+  uint64_t hbm_cap_bytes;  /* resident matrices + query scratch never exceed this
+                            * (the library's pool may keep up to 4 GiB of freed
+                            * memory mapped on top of it)                        */
 } eh_server_config;
 typedef enum eh_query_kind {
   EH_QUERY_TRIANGLES = 0,     /* param unused                                    */
