@@ -44,6 +44,12 @@ typedef struct {
   uint64_t num_uint, num_pshort, num_bitset;
 } omatrix;
 
+/* The reference's flattened rows put u32 elements at any byte offset (the
+ * hybrid tag and byte-count headers shift them, hybrid.hpp:132-201): uint rows
+ * are read and written through this type, whose loads are defined at any
+ * alignment. */
+typedef uint32_t u32u __attribute__((aligned(1), may_alias));
+
 static inline uint64_t rd64(const uint8_t* p) { uint64_t v; memcpy(&v, p, 8); return v; }
 static inline uint32_t rd32(const uint8_t* p) { uint32_t v; memcpy(&v, p, 4); return v; }
 static inline uint16_t rd16(const uint8_t* p) { uint16_t v; memcpy(&v, p, 2); return v; }
@@ -198,8 +204,7 @@ static oset get_row(const omatrix* m, uint64_t i) {
 
 /* Merge of two sorted u32 arrays: ops::scalar (intersection.hpp:46-79); also the
  * result of set_intersect_standard's 4x4 block compare (:696-771). */
-static uint64_t merge_u32(const uint32_t* a, uint64_t la, const uint32_t* b, uint64_t lb,
-                          uint32_t* out) {
+static uint64_t merge_u32(const u32u* a, uint64_t la, const u32u* b, uint64_t lb, u32u* out) {
   uint64_t i = 0, j = 0, c = 0;
   while (i < la && j < lb) {
     if (a[i] < b[j]) i++;
@@ -213,8 +218,7 @@ static uint64_t merge_u32(const uint32_t* a, uint64_t la, const uint32_t* b, uin
 }
 /* set_intersect_galloping (intersection.hpp:393-584): each rare element is located
  * in freq by an exponential then binary search from the previous position. */
-static uint64_t gallop_u32(const uint32_t* rare, uint64_t lr, const uint32_t* freq, uint64_t lf,
-                           uint32_t* out) {
+static uint64_t gallop_u32(const u32u* rare, uint64_t lr, const u32u* freq, uint64_t lf, u32u* out) {
   uint64_t lo = 0, c = 0;
   for (uint64_t i = 0; i < lr && lo < lf; i++) {
     uint32_t x = rare[i];
@@ -240,18 +244,16 @@ static uint64_t ix_uu(oset A, oset B, uint8_t* out) {
   const oset* freq = (A.card > B.card) ? &A : &B;
   uint64_t mn = rare->card ? rare->card : 1;
   if (freq->card / mn > 32)
-    return gallop_u32((const uint32_t*)rare->data, rare->card, (const uint32_t*)freq->data,
-                      freq->card, (uint32_t*)out);
-  return merge_u32((const uint32_t*)rare->data, rare->card, (const uint32_t*)freq->data,
-                   freq->card, (uint32_t*)out);
+    return gallop_u32((const u32u*)rare->data, rare->card, (const u32u*)freq->data, freq->card, (u32u*)out);
+  return merge_u32((const u32u*)rare->data, rare->card, (const u32u*)freq->data, freq->card, (u32u*)out);
 }
 /* set_intersect(uint, bitset) (intersection.hpp:1023-1058): probe each uint element,
  * stop at the first element past the bitset's last word. */
 static uint64_t ix_ub(oset A, oset B, uint8_t* out) {
   uint64_t sb = B.nbytes > 0 ? (B.nbytes - 8) / 8 : 0;
   uint64_t start = B.nbytes > 0 ? rd64(B.data) : 0;
-  const uint32_t* a = (const uint32_t*)A.data;
-  uint32_t* o = (uint32_t*)out;
+  const u32u* a = (const u32u*)A.data;
+  u32u* o = (u32u*)out;
   uint64_t c = 0;
   for (uint64_t i = 0; i < A.card; i++) {
     uint64_t w = a[i] >> 6;
@@ -366,8 +368,8 @@ static uint64_t ix_pb(oset A, oset B, uint8_t* out, uint64_t* out_nbytes) {
 /* set_intersect(uint, pshort) (intersection.hpp:1062-1173): partition-aware merge.
  * Result layout uint. */
 static uint64_t ix_up(oset A, oset B, uint8_t* out) {
-  const uint32_t* a = (const uint32_t*)A.data;
-  uint32_t* o = (uint32_t*)out;
+  const u32u* a = (const u32u*)A.data;
+  u32u* o = (u32u*)out;
   uint64_t sb = B.nbytes / 2, ai = 0, bi = 0, c = 0;
   while (ai < A.card && bi < sb) {
     uint32_t prefix = (uint32_t)rd16(B.data + 2 * bi) << 16;

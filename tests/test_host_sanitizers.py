@@ -1,7 +1,8 @@
 """The host half of the engine (loaders, generators, reordering, directed
-graphs: csrc/eh_host.cpp) under AddressSanitizer + UndefinedBehaviorSanitizer,
-built apart from the CUDA code.  (compute-sanitizer, the device-side
-counterpart, is not available on the GPU pool.)"""
+graphs: csrc/eh_host.cpp) and the C oracle (oracle/eh_oracle.c) under
+AddressSanitizer + UndefinedBehaviorSanitizer, built apart from the CUDA code.
+(compute-sanitizer, the device-side counterpart, is not available on the GPU
+pool.)"""
 import os
 import subprocess
 
@@ -24,3 +25,17 @@ def test_host_code_is_clean_under_asan_ubsan(tmp_path):
     r = subprocess.run([exe, str(tmp_path)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, env=env,
                        timeout=300)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout[-3000:]
+
+
+def test_oracle_is_clean_under_asan_ubsan(tmp_path):
+    exe = str(tmp_path / "oracle_asan")
+    cmd = ["gcc", "-std=c99", "-O1", "-g", "-fopenmp", "-fsanitize=address,undefined",
+           "-fno-sanitize-recover=undefined", os.path.join(ROOT, "oracle", "eh_oracle.c"),
+           os.path.join(ROOT, "tests", "cpp", "oracle_asan.c"), "-o", exe]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0 and ("cannot find -lasan" in r.stdout or "libasan" in r.stdout):
+        pytest.skip("sanitizer runtime not installed")
+    assert r.returncode == 0, r.stdout[-3000:]
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1", OMP_NUM_THREADS="2")
+    r = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, env=env, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().splitlines()[-1].startswith("ok"), r.stdout[-3000:]
