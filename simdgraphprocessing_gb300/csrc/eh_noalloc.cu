@@ -94,7 +94,9 @@ extern "C" eh_status eh_count_cliques_noalloc(eh_matrix_t mh, uint32_t k, uint64
   uint32_t* counters = scratch;
   uint32_t* slots = scratch + kCounterWords;
   const uint64_t slot_capacity = kNoAllocScratchWords - kCounterWords;
-  CliqueArgs a{m->desc, m->arena, p.order, k, reinterpret_cast<unsigned long long*>(d_count), nullptr, 0};
+  // No dense core here: the counts probe the rows themselves.
+  CliqueArgs a{m->desc, m->arena, p.order, k, reinterpret_cast<unsigned long long*>(d_count), nullptr, 0,
+               nullptr, 0};
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
   uint64_t grid_g = 0;
