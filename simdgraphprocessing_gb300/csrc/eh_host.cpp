@@ -40,18 +40,29 @@ void clear_error() { g_last_error.clear(); }
 void csr_from_undirected_keys(uint64_t n, std::vector<uint64_t>& keys, HostGraph& g) {
   g.n = n;
   g.offsets.assign(n + 1, 0);
-  std::vector<uint64_t> deg(n, 0);
-  for (uint64_t k : keys) {
-    deg[k >> 32]++;
-    deg[k & 0xffffffffu]++;
+  const int64_t m = (int64_t)keys.size();
+  const uint64_t* kp = keys.data();
+  {
+    std::vector<uint64_t> deg(n, 0);
+    uint64_t* dp = deg.data();
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < m; k++) {
+      __atomic_fetch_add(&dp[kp[k] >> 32], 1, __ATOMIC_RELAXED);
+      __atomic_fetch_add(&dp[kp[k] & 0xffffffffu], 1, __ATOMIC_RELAXED);
+    }
+    for (uint64_t i = 0; i < n; i++) g.offsets[i + 1] = g.offsets[i] + deg[i];
   }
-  for (uint64_t i = 0; i < n; i++) g.offsets[i + 1] = g.offsets[i] + deg[i];
-  g.nbrs.assign(g.offsets[n], 0);
+  // Both directions of every edge, placed by atomic row cursors; each row is
+  // sorted below, so the result does not depend on the order of placement.
+  g.nbrs.resize(g.offsets[n]);
   std::vector<uint64_t> cur(g.offsets.begin(), g.offsets.end() - 1);
-  for (uint64_t k : keys) {
-    uint32_t lo = (uint32_t)(k >> 32), hi = (uint32_t)(k & 0xffffffffu);
-    g.nbrs[cur[lo]++] = hi;
-    g.nbrs[cur[hi]++] = lo;
+  uint64_t* cp = cur.data();
+  uint32_t* np = g.nbrs.data();
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < m; k++) {
+    const uint32_t lo = (uint32_t)(kp[k] >> 32), hi = (uint32_t)(kp[k] & 0xffffffffu);
+    np[__atomic_fetch_add(&cp[lo], 1, __ATOMIC_RELAXED)] = hi;
+    np[__atomic_fetch_add(&cp[hi], 1, __ATOMIC_RELAXED)] = lo;
   }
   std::vector<uint64_t>().swap(keys);
 #pragma omp parallel for schedule(dynamic, 1024)
@@ -88,6 +99,32 @@ static inline uint64_t ukey(uint64_t u, uint64_t v) {
 }
 static const uint64_t kSelfLoop = ~0ULL;
 
+// Order-preserving parallel compaction: out receives, in order, the elements
+// e of in[0, n) with keep(k) true for their index k; returns how many.
+template <class T, class Keep>
+static uint64_t compact(const T* in, uint64_t n, Keep keep, T* out) {
+  std::vector<uint64_t> start(omp_get_max_threads() + 1, 0);
+  uint64_t kept = 0;
+#pragma omp parallel
+  {
+    const uint64_t t = omp_get_thread_num(), nt = omp_get_num_threads();  // the team actually started
+    const uint64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+    uint64_t c = 0;
+    for (uint64_t k = lo; k < hi; k++) c += keep(k) ? 1 : 0;
+    start[t + 1] = c;
+#pragma omp barrier
+#pragma omp single
+    {
+      for (uint64_t i = 0; i < nt; i++) start[i + 1] += start[i];
+      kept = start[nt];
+    }
+    uint64_t pos = start[t];
+    for (uint64_t k = lo; k < hi; k++)
+      if (keep(k)) out[pos++] = in[k];
+  }
+  return kept;
+}
+
 // Keeps the first `target` distinct keys in draw order.  `draw(lo, hi, out)`
 // fills out[k - lo] for draws k in [lo, hi) (kSelfLoop for draws to discard).
 template <class Draw>
@@ -109,30 +146,43 @@ static bool first_distinct(uint64_t target, uint64_t first_batch, Draw draw,
     __gnu_parallel::sort(v.begin(), v.end(), [](const KI& a, const KI& b) {
       return a.key < b.key || (a.key == b.key && a.idx < b.idx);
     });
-    std::vector<KI> heads;
-    heads.reserve(total);
-    for (uint64_t k = 0; k < total; k++) {
-      if (v[k].key == kSelfLoop) break;  // kSelfLoop sorts last
-      if (k == 0 || v[k].key != v[k - 1].key) heads.push_back(v[k]);
-    }
-    if (heads.size() >= target) {
-      std::vector<uint64_t> idx(heads.size());
-      for (size_t h = 0; h < heads.size(); h++) idx[h] = heads[h].idx;
+    // The first draw of every distinct key (self-loops, which sort last, dropped).
+    std::vector<KI> heads(total);
+    const KI* vp = v.data();
+    const uint64_t nh = compact(vp, total, [vp](uint64_t k) {
+      return vp[k].key != kSelfLoop && (k == 0 || vp[k].key != vp[k - 1].key);
+    }, heads.data());
+    heads.resize(nh);
+    std::vector<KI>().swap(v);
+    if (nh >= target) {
+      // cutoff = the target-th smallest first-draw index: mark the heads' indices
+      // in a bitmap of all draws and walk its popcounts.
       uint64_t cutoff = ~0ULL;
       if (target > 0) {
-        std::nth_element(idx.begin(), idx.begin() + (target - 1), idx.end());
-        cutoff = idx[target - 1];
+        const uint64_t nw = (total + 63) / 64;
+        std::vector<uint64_t> bits(nw, 0);
+#pragma omp parallel for schedule(static)
+        for (int64_t h = 0; h < (int64_t)nh; h++)
+          __atomic_fetch_or(&bits[heads[h].idx >> 6], 1ULL << (heads[h].idx & 63), __ATOMIC_RELAXED);
+        uint64_t seen = 0, w = 0;
+        while (seen + (uint64_t)__builtin_popcountll(bits[w]) < target) seen += __builtin_popcountll(bits[w++]);
+        uint64_t x = bits[w];
+        for (uint64_t r = target - seen; r > 1; r--) x &= x - 1;  // drop the lowest r - 1 set bits
+        cutoff = 64 * w + (uint64_t)__builtin_ctzll(x);
       }
-      result.clear();
-      result.reserve(target);
-      if (target > 0)
-        for (const KI& h : heads)
-          if (h.idx <= cutoff) result.push_back(h.key);
+      result.resize(nh);
+      const KI* hp = heads.data();
+      std::vector<uint64_t> keys(nh);
+#pragma omp parallel for schedule(static)
+      for (int64_t h = 0; h < (int64_t)nh; h++) keys[h] = hp[h].key;
+      const uint64_t kept = compact(keys.data(), nh, [hp, cutoff](uint64_t h) { return hp[h].idx <= cutoff; },
+                                    result.data());
+      result.resize(kept);
       return true;  // result is sorted by key
     }
     // Grow the draw count in proportion to the shortfall.
-    double yield = (double)heads.size() / (double)total;
-    uint64_t need = (uint64_t)((double)(target - heads.size()) / std::max(yield, 1e-3) * 1.2) + 1024;
+    double yield = (double)nh / (double)total;
+    uint64_t need = (uint64_t)((double)(target - nh) / std::max(yield, 1e-3) * 1.2) + 1024;
     batch = need;
   }
   return false;
