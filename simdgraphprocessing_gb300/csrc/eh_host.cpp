@@ -207,6 +207,35 @@ static uint64_t max_row(const std::vector<uint64_t>& off) {
   return mx;
 }
 
+// Whole file into buf: 0 on success, -1 if it cannot be opened, 1 if it cannot
+// be read to the end.
+static int read_whole_file(const char* path, std::vector<uint8_t>& buf) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return -1;
+  bool ok = fseeko(f, 0, SEEK_END) == 0;
+  const off_t size = ok ? ftello(f) : -1;
+  ok = ok && size >= 0 && fseeko(f, 0, SEEK_SET) == 0;
+  if (ok) {
+    buf.resize((size_t)size);
+    ok = size == 0 || fread(buf.data(), 1, (size_t)size, f) == (size_t)size;
+  }
+  fclose(f);
+  return ok ? 0 : 1;
+}
+
+// Bounds-checked little-endian reads from a byte buffer.
+struct ByteCursor {
+  const uint8_t* p;
+  uint64_t size, pos;
+  uint64_t left() const { return size - pos; }
+  bool take64(uint64_t& v) {
+    if (left() < 8) return false;
+    memcpy(&v, p + pos, 8);
+    pos += 8;
+    return true;
+  }
+};
+
 static eh_status finish_graph(uint64_t n, std::vector<uint64_t>& keys, eh_hgraph_t* out) {
   HostGraph* g = new (std::nothrow) HostGraph();
   if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
@@ -271,36 +300,40 @@ eh_status eh_hgraph_from_csr(uint64_t n, const uint64_t* offsets, const uint32_t
 
 eh_status eh_hgraph_read_binary(const char* path, eh_hgraph_t* out) {
   EH_CHECK_ARG(path && out, "path/out is NULL");
-  FILE* f = fopen(path, "rb");
-  if (!f) return set_error(EH_ERR_IO, "cannot open %s", path);
+  std::vector<uint8_t> buf;
+  const int rf = eh::read_whole_file(path, buf);
+  if (rf < 0) return set_error(EH_ERR_IO, "cannot open %s", path);
   HostGraph* g = new (std::nothrow) HostGraph();
-  if (!g) {
-    fclose(f);
-    return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
-  }
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
+  // Records: [u64 ext_id][u64 len][u32 x len].  One pass finds every row's
+  // neighbours in the file, then the rows are copied in parallel.
+  eh::ByteCursor in{buf.data(), rf == 0 ? buf.size() : 0, 0};
   uint64_t n = 0;
-  bool ok = fread(&n, sizeof(n), 1, f) == 1 && n < (1ULL << 32);
+  bool ok = in.take64(n) && n < (1ULL << 32) && n <= in.left() / 16;
+  std::vector<uint64_t> at;
   if (ok) {
     g->n = n;
     g->offsets.assign(n + 1, 0);
     g->ext_ids.resize(n);
+    at.resize(n);
     for (uint64_t i = 0; i < n && ok; i++) {
-      uint64_t hdr[2];
-      ok = fread(hdr, sizeof(uint64_t), 2, f) == 2;
+      uint64_t len = 0;
+      ok = in.take64(g->ext_ids[i]) && in.take64(len) && len <= in.left() / 4;
       if (!ok) break;
-      g->ext_ids[i] = hdr[0];
-      g->offsets[i + 1] = g->offsets[i] + hdr[1];
-      g->max_nbrhood_size = std::max(g->max_nbrhood_size, hdr[1]);
-      size_t at = g->nbrs.size();
-      g->nbrs.resize(at + hdr[1]);
-      if (hdr[1]) ok = fread(g->nbrs.data() + at, sizeof(uint32_t), hdr[1], f) == hdr[1];
+      at[i] = in.pos;
+      in.pos += 4 * len;
+      g->offsets[i + 1] = g->offsets[i] + len;
+      g->max_nbrhood_size = std::max(g->max_nbrhood_size, len);
     }
   }
-  fclose(f);
   if (!ok) {
     delete g;
     return set_error(EH_ERR_IO, "truncated or malformed binary graph %s", path);
   }
+  g->nbrs.resize(g->offsets[n]);
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t i = 0; i < (int64_t)n; i++)
+    memcpy(g->nbrs.data() + g->offsets[i], buf.data() + at[i], 4 * (g->offsets[i + 1] - g->offsets[i]));
   *out = reinterpret_cast<eh_hgraph_t>(g);
   return EH_OK;
 }
@@ -429,44 +462,55 @@ void eh_hgraph_free(eh_hgraph_t g) { delete HG(g); }
 
 eh_status eh_hgraph_read_directed_binary(const char* path, eh_hgraph_t* out) {
   EH_CHECK_ARG(path && out, "path/out is NULL");
-  FILE* f = fopen(path, "rb");
-  if (!f) return set_error(EH_ERR_IO, "cannot open %s", path);
+  std::vector<uint8_t> buf;
+  const int rf = eh::read_whole_file(path, buf);
+  if (rf < 0) return set_error(EH_ERR_IO, "cannot open %s", path);
   HostGraph* g = new (std::nothrow) HostGraph();
-  if (!g) {
-    fclose(f);
-    return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
-  }
+  if (!g) return set_error(EH_ERR_OUT_OF_MEMORY, "host graph allocation failed");
   g->directed = true;
+  // Records: [u64 ext_id][u64 out_len][u32 x out_len][u64 in_len][u32 x in_len].
+  eh::ByteCursor in{buf.data(), rf == 0 ? buf.size() : 0, 0};
   uint64_t n = 0;
-  bool ok = fread(&n, sizeof(n), 1, f) == 1 && n < (1ULL << 32);
+  bool ok = in.take64(n) && n < (1ULL << 32) && n <= in.left() / 24;
+  std::vector<uint64_t> at_out, at_in;
   if (ok) {
     g->n = n;
     g->offsets.assign(n + 1, 0);
     g->in_offsets.assign(n + 1, 0);
     g->ext_ids.resize(n);
+    at_out.resize(n);
+    at_in.resize(n);
     for (uint64_t i = 0; i < n && ok; i++) {
-      uint64_t hdr[2], len = 0;
-      ok = fread(hdr, sizeof(uint64_t), 2, f) == 2;
+      uint64_t len = 0, in_len = 0;
+      ok = in.take64(g->ext_ids[i]) && in.take64(len) && len <= in.left() / 4;
       if (!ok) break;
-      g->ext_ids[i] = hdr[0];
-      g->offsets[i + 1] = g->offsets[i] + hdr[1];
-      size_t at = g->nbrs.size();
-      g->nbrs.resize(at + hdr[1]);
-      if (hdr[1]) ok = fread(g->nbrs.data() + at, sizeof(uint32_t), hdr[1], f) == hdr[1];
-      ok = ok && fread(&len, sizeof(uint64_t), 1, f) == 1;
+      at_out[i] = in.pos;
+      in.pos += 4 * len;
+      ok = in.take64(in_len) && in_len <= in.left() / 4;
       if (!ok) break;
-      g->in_offsets[i + 1] = g->in_offsets[i] + len;
-      at = g->in_nbrs.size();
-      g->in_nbrs.resize(at + len);
-      if (len) ok = fread(g->in_nbrs.data() + at, sizeof(uint32_t), len, f) == len;
-      g->max_nbrhood_size = std::max(g->max_nbrhood_size, std::max(hdr[1], len));
+      at_in[i] = in.pos;
+      in.pos += 4 * in_len;
+      g->offsets[i + 1] = g->offsets[i] + len;
+      g->in_offsets[i + 1] = g->in_offsets[i] + in_len;
+      g->max_nbrhood_size = std::max(g->max_nbrhood_size, std::max(len, in_len));
     }
   }
-  fclose(f);
-  if (ok)
-    for (uint32_t v : g->nbrs) ok = ok && v < n;
-  if (ok)
-    for (uint32_t v : g->in_nbrs) ok = ok && v < n;
+  if (ok) {
+    g->nbrs.resize(g->offsets[n]);
+    g->in_nbrs.resize(g->in_offsets[n]);
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+      uint32_t* o = g->nbrs.data() + g->offsets[i];
+      uint32_t* r = g->in_nbrs.data() + g->in_offsets[i];
+      const uint64_t lo = g->offsets[i + 1] - g->offsets[i], li = g->in_offsets[i + 1] - g->in_offsets[i];
+      memcpy(o, buf.data() + at_out[i], 4 * lo);
+      memcpy(r, buf.data() + at_in[i], 4 * li);
+      for (uint64_t k = 0; k < lo; k++) bad |= o[k] >= n;
+      for (uint64_t k = 0; k < li; k++) bad |= r[k] >= n;
+    }
+    ok = !bad;
+  }
   if (!ok) {
     delete g;
     return set_error(EH_ERR_IO, "truncated or malformed directed binary graph %s", path);
