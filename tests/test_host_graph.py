@@ -55,6 +55,35 @@ def test_truncated_binary_is_an_io_error(eh, tmp_path):
     assert e.value.status == 5
 
 
+def test_malformed_binary_headers_are_io_errors(eh, tmp_path):
+    """Record counts and row lengths that the file cannot hold are rejected
+    before anything of that size is allocated; a missing file is an I/O error
+    too; trailing bytes after the last record are ignored, as before."""
+    import struct
+    p = str(tmp_path / "bad.bin")
+    cases = [
+        struct.pack("<Q", 1 << 31),                                   # 2^31 rows, no records
+        struct.pack("<QQQ", 1, 0, 1 << 60),                          # one row of 2^60 entries
+        struct.pack("<QQQ", 2, 0, 1) + struct.pack("<I", 1),         # second record missing
+        struct.pack("<Q", 1 << 40),                                   # n beyond the u32 id space
+        b"\x01\x00",                                                  # shorter than the header
+    ]
+    for blob in cases:
+        open(p, "wb").write(blob)
+        for reader in (eh.HostGraph.read_binary, eh.HostGraph.read_directed_binary):
+            with pytest.raises(eh.EHError) as e:
+                reader(p)
+            assert e.value.status == 5, (blob, reader)
+    with pytest.raises(eh.EHError) as e:
+        eh.HostGraph.read_binary(str(tmp_path / "missing.bin"))
+    assert e.value.status == 5
+    g = eh.graph("er", 4, n=100, edges=300)
+    g.write_binary(p)
+    open(p, "ab").write(b"trailing bytes")
+    h = eh.HostGraph.read_binary(p)
+    assert all(np.array_equal(x, y) for x, y in zip(g.csr()[:3], h.csr()[:3]))
+
+
 def test_edge_list_semantics(eh, tmp_path):
     # undirectedFromEdgeList (src/MutableGraph.hpp:517-599): ids in order of first
     # appearance, both directions, sorted + deduplicated rows, self-loops kept,
