@@ -397,6 +397,9 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
   // The reference's recursion only returns a count at depth n >= 3 (apps/n_clique.cpp:41-43);
   // for n < 3 it never reaches that depth and the count stays 0.
   if (k < 3) return EH_OK;
+  if (m->tot.max_card >= kCliqueMaxPivot)
+    return set_error(EH_ERR_UNSUPPORTED, "a row of %llu selected entries is above the clique kernels' limit of %u",
+                     (unsigned long long)m->tot.max_card, kCliqueMaxPivot - 1);
   eh_status s = ensure_plan(m, st);
   if (s != EH_OK) return s;
   const Plan& p = m->plan;

@@ -136,6 +136,10 @@ struct CliqueArgs {
   uint32_t core_k;
 };
 constexpr uint32_t kCliqueMaxK = 16;
+// Largest pivot row a clique count accepts: a pivot's packed masks are indexed
+// with 32-bit word offsets, which stay exact below 2^18 entries (a degree-
+// ordered graph reaches that only past 2^35 edges).
+constexpr uint32_t kCliqueMaxPivot = 1u << 18;
 constexpr uint32_t kCliqueSmemMax = 2048;  // no pivot above this size keeps its masks in shared memory
 // Words of one pivot's working set (list, masks, per-warp DFS stacks).
 uint64_t clique_slot_words(uint32_t cmax, uint32_t k);

@@ -86,6 +86,9 @@ extern "C" eh_status eh_count_cliques_noalloc(eh_matrix_t mh, uint32_t k, uint64
   cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(uint64_t), st);
   if (e != cudaSuccess) return set_error(EH_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
   if (k < 3) return EH_OK;  // as eh_count_cliques: the reference returns 0 for n < 3
+  if (m->tot.max_card >= kCliqueMaxPivot)
+    return set_error(EH_ERR_UNSUPPORTED, "a row of %llu selected entries is above the clique kernels' limit of %u",
+                     (unsigned long long)m->tot.max_card, kCliqueMaxPivot - 1);
   const Plan& p = m->plan;
   const uint32_t cap = clique_smem_cap(k, m->device);
   const uint32_t nG = p.above(cap);

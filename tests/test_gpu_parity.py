@@ -157,6 +157,28 @@ def test_chunked_host_upload_equals_device_build(eh):
     assert "offsets" in str(ei.value)
 
 
+def test_clique_pivot_limit_is_an_error_before_any_launch(eh):
+    """A star whose centre has the highest id keeps all n - 1 > 2^18 leaves in
+    one selected row: clique counts reject it (EH_ERR_UNSUPPORTED) before any
+    kernel runs, since the packed masks' 32-bit offsets are exact only below
+    2^18 entries; the triangle count of the same matrix is still 0."""
+    n = (1 << 18) + 8
+    hub = n - 1
+    deg = np.ones(n, np.uint64)
+    deg[hub] = n - 1
+    off = np.zeros(n + 1, np.uint64)
+    off[1:] = np.cumsum(deg)
+    nbr = np.empty(int(off[-1]), np.uint32)
+    nbr[:n - 1] = hub
+    nbr[n - 1:] = np.arange(n - 1, dtype=np.uint32)
+    m = eh.Matrix.build(off, nbr, selection="lower", layout="hybrid")
+    assert m.info()["max_row_cardinality"] == n - 1
+    with pytest.raises(eh.EHError) as ei:
+        m.count_cliques(4)
+    assert ei.value.status == 4
+    assert m.count_triangles() == 0
+
+
 def test_empty_and_tiny_graphs(eh, oracle):
     for off, nbr in [(np.zeros(1, np.uint64), np.zeros(0, np.uint32)),
                      (np.zeros(5, np.uint64), np.zeros(0, np.uint32)),
