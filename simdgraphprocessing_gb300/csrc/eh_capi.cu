@@ -527,27 +527,15 @@ eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* n
   // The adjacency goes up in chunks of rows (about kUploadChunkEntries entries
   // each) on the upload stream, and the build's first pass measures each chunk
   // as soon as it has landed, so the copy over the host link and the measure
-  // pass overlap.  Chunk boundaries come from a binary search of the host
-  // offsets; the byte ranges are clamped to stay monotone within [0, m) so
-  // that every entry is copied exactly once whatever the offsets hold (rows
-  // with bad offsets are rejected by the measure pass).
+  // pass overlap.  Every entry is copied exactly once whatever the offsets
+  // hold (rows with bad offsets are rejected by the measure pass).
   constexpr uint64_t kUploadChunkEntries = 16ull << 20;
   constexpr uint64_t kUploadMaxChunks = 16;
   const uint64_t chunks =
       std::max<uint64_t>(1, std::min<uint64_t>(kUploadMaxChunks, (m + kUploadChunkEntries - 1) / kUploadChunkEntries));
   eh::UploadChunks up;
-  up.rows.push_back(0);
-  for (uint64_t c = 1; c < chunks; c++) {
-    const uint64_t target = m / chunks * c;
-    uint64_t lo = 0, hi = n;  // first row whose offset reaches target
-    while (lo < hi) {
-      const uint64_t mid = lo + (hi - lo) / 2;
-      if (offsets[mid] < target) lo = mid + 1;
-      else hi = mid;
-    }
-    up.rows.push_back(std::max(lo, up.rows.back()));
-  }
-  up.rows.push_back(n);
+  std::vector<uint64_t> upto;
+  eh::plan_upload_chunks(n, offsets, m, chunks, up.rows, upto);
   eh_status s = EH_OK;
   cudaEvent_t allocated = nullptr;
   auto event = [](cudaEvent_t* ev) { return cudaEventCreateWithFlags(ev, cudaEventDisableTiming); };
@@ -558,17 +546,16 @@ eh_status eh_matrix_build(uint64_t n, const uint64_t* offsets, const uint32_t* n
     s = eh::cuda_fail(e, "upload");
   uint64_t copied = 0;
   for (uint64_t c = 0; c < chunks && s == EH_OK; c++) {
-    const uint64_t upto = c + 1 == chunks ? m : std::min(m, std::max(copied, offsets[up.rows[c + 1]]));
-    if (upto > copied) {
-      if ((e = cudaMemcpyAsync(d_nbr + copied, nbrs + copied, (upto - copied) * 4, cudaMemcpyHostToDevice, cs)) !=
-              cudaSuccess ||
-          (d_mask && (e = cudaMemcpyAsync(d_mask + copied, edge_mask + copied, upto - copied, cudaMemcpyHostToDevice,
-                                          cs)) != cudaSuccess)) {
+    if (upto[c] > copied) {
+      if ((e = cudaMemcpyAsync(d_nbr + copied, nbrs + copied, (upto[c] - copied) * 4, cudaMemcpyHostToDevice,
+                               cs)) != cudaSuccess ||
+          (d_mask && (e = cudaMemcpyAsync(d_mask + copied, edge_mask + copied, upto[c] - copied,
+                                          cudaMemcpyHostToDevice, cs)) != cudaSuccess)) {
         s = eh::cuda_fail(e, "upload");
         break;
       }
     }
-    copied = upto;
+    copied = upto[c];
     cudaEvent_t ev = nullptr;
     if ((e = event(&ev)) != cudaSuccess) {
       s = eh::cuda_fail(e, "upload event");

@@ -75,6 +75,29 @@ void csr_from_undirected_keys(uint64_t n, std::vector<uint64_t>& keys, HostGraph
   std::iota(g.ext_ids.begin(), g.ext_ids.end(), 0);
 }
 
+void plan_upload_chunks(uint64_t n, const uint64_t* offsets, uint64_t m, uint64_t chunks,
+                        std::vector<uint64_t>& rows, std::vector<uint64_t>& upto) {
+  if (chunks < 1) chunks = 1;
+  rows.assign(1, 0);
+  for (uint64_t c = 1; c < chunks; c++) {
+    const uint64_t target = m / chunks * c;
+    uint64_t lo = 0, hi = n;  // first row whose offset reaches target
+    while (lo < hi) {
+      const uint64_t mid = lo + (hi - lo) / 2;
+      if (offsets[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    rows.push_back(std::max(lo, rows.back()));
+  }
+  rows.push_back(n);
+  upto.assign(chunks, 0);
+  uint64_t copied = 0;
+  for (uint64_t c = 0; c < chunks; c++) {
+    copied = c + 1 == chunks ? m : std::min(m, std::max(copied, offsets[rows[c + 1]]));
+    upto[c] = copied;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Counter-based random stream: value(k) = SplitMix64 finalizer applied to
 // key + (k+1) * golden-gamma (Steele, Lea, Flood, "Fast splittable

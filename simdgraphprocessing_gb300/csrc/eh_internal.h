@@ -31,6 +31,15 @@ struct HostGraph {
 // `keys` is consumed.  Rows come out sorted ascending.
 void csr_from_undirected_keys(uint64_t n, std::vector<uint64_t>& keys, HostGraph& g);
 
+// Split of a host adjacency (n rows, m = offsets[n] entries) into `chunks`
+// uploads of about m / chunks entries: chunk c holds rows [rows[c], rows[c+1])
+// and is complete once entries [0, upto[c]) have been copied.  rows runs from
+// 0 to n and upto from its first value to m, both non-decreasing whatever the
+// offsets hold (a binary search of the offsets places the boundaries; rows
+// with bad offsets are for the device pass to reject).
+void plan_upload_chunks(uint64_t n, const uint64_t* offsets, uint64_t m, uint64_t chunks,
+                        std::vector<uint64_t>& rows, std::vector<uint64_t>& upto);
+
 }  // namespace eh
 
 #define EH_CHECK_ARG(cond, ...)                                      \
