@@ -1,11 +1,51 @@
 """Shared helpers for the committed reference fixtures (tests/golden/)."""
+import gzip
 import hashlib
 import json
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "golden", "reference_counts.json")
-REFERENCE_TREE = os.environ.get("EH_REFERENCE", "/root/reference")
+LARGE_FIXTURE = os.path.join(HERE, "golden", "reference_large.json")
+# The reference source tree, for the tests that compile its sources (set
+# EH_REFERENCE to its path; those tests are skipped without it).
+REFERENCE_TREE = os.environ.get("EH_REFERENCE") or None
+
+# The reference's own test graphs (its test/data/facebook.bin and
+# test/data/dfacebook.bin, byte for byte, gzip-compressed) and their SHA-256.
+FACEBOOK = {
+    "facebook.bin": "7be683d99952d5ff0ade026151d2f42d576fc9373309688e65ccdcfee183843e",
+    "dfacebook.bin": "e6100bd8fe240b283f4679de69175acf93ea400ecc46f6e0b33ffadc0960c286",
+}
+
+
+def reference_file(*parts):
+    """Path of a file in the reference tree, or None without EH_REFERENCE."""
+    if not REFERENCE_TREE:
+        return None
+    p = os.path.join(REFERENCE_TREE, *parts)
+    return p if os.path.exists(p) else None
+
+
+def fixture_graph(name, directory):
+    """Writes the reference test graph `name` (facebook.bin / dfacebook.bin)
+    into `directory` and returns its path, after checking its SHA-256."""
+    with gzip.open(os.path.join(HERE, "golden", name + ".gz"), "rb") as f:
+        data = f.read()
+    assert hashlib.sha256(data).hexdigest() == FACEBOOK[name], name
+    path = os.path.join(str(directory), name)
+    with open(path, "wb") as f:
+        f.write(data)
+    return path
+
+
+def load_large():
+    with open(LARGE_FIXTURE) as f:
+        return json.load(f)
+
+
+def large_graph(name):
+    return next(g for g in load_large()["graphs"] if g["name"] == name)
 
 
 def load():

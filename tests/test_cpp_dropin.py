@@ -1,9 +1,12 @@
 """The drop-in C++ host API (simdgraphprocessing_gb300/host + apps).
 
 CPU: the reference's own gtest sources for the hot path compile unmodified
-against the drop-in headers (when the reference tree is present).
-GPU: a C++ driver that uses the app classes exactly as those gtests do runs on
-fixture graphs and must reproduce the reference binaries' counts.
+against the drop-in headers (with EH_REFERENCE naming the reference tree).
+GPU: the reference's seven gtests restated without gtest (tests/cpp/
+dropin_gtests.cpp: same loaders, Parser arguments, app classes and expected
+values) run on the reference's own test graphs (committed under tests/golden/),
+and a C++ driver that uses the app classes the same way reproduces the
+reference binaries' counts on the seeded fixture graphs.
 """
 import os
 import subprocess
@@ -21,8 +24,8 @@ REF_TESTS = ["undirected_triangle_counting_test", "n_clique_test", "undirected_l
              "similar_nodes_test", "symbiosity_test", "n_path_test"]
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(_golden.REFERENCE_TREE, "test")),
-                    reason="reference tree not present")
+@pytest.mark.skipif(_golden.reference_file("test") is None,
+                    reason="EH_REFERENCE does not name the reference tree")
 @pytest.mark.parametrize("name", REF_TESTS)
 def test_reference_gtests_compile_against_dropin_headers(name):
     ref = _golden.REFERENCE_TREE
@@ -65,6 +68,21 @@ def test_host_set_ops(tmp_path):
 def test_dropin_driver_compiles(tmp_path, eh):
     _build_driver(tmp_path, eh)
     _build_driver(tmp_path, eh, "dropin_directed")
+    _build_driver(tmp_path, eh, "dropin_gtests")
+
+
+@pytest.mark.gpu
+def test_reference_gtests_on_gpu(tmp_path, eh):
+    """The reference's gtest goldens (1,612,010 triangles; 30,004,668
+    4-cliques; 713,455,740 lollipops; 904 similar nodes; symbiosity 0 directed
+    and 4,039 undirected; BFS path length 4) from the GPU through the drop-in
+    C++ API."""
+    exe = _build_driver(tmp_path, eh, "dropin_gtests")
+    for name in _golden.FACEBOOK:
+        _golden.fixture_graph(name, tmp_path)
+    r = subprocess.run([exe, str(tmp_path)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert "7 of 7 passed" in r.stdout
 
 
 @pytest.mark.gpu

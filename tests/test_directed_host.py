@@ -3,8 +3,8 @@
 * MutableGraph::directedFromBinary / writeDirectedToBinary /
   directedFromEdgeList (src/MutableGraph.hpp:634-714, 893-986) restated by
   eh_hgraph_*_directed_*; checked against a plain-Python reading of the format
-  and, when the reference tree is present, byte for byte on its
-  test/data/dfacebook.bin.
+  and byte for byte on the reference's test/data/dfacebook.bin (committed as
+  tests/golden/dfacebook.bin.gz).
 * The oracle's symbiosity (apps/symbiosity.cpp:39-58) and n_path
   (apps/n_path.cpp:30-88) pinned to the reference's gtest goldens
   (test/symbiosity_test.cpp:6-20, test/n_path_test.cpp:6-12) and to the
@@ -19,8 +19,6 @@ import pytest
 
 import _golden
 
-DFB = os.path.join(_golden.REFERENCE_TREE, "test", "data", "dfacebook.bin")
-FB = os.path.join(_golden.REFERENCE_TREE, "test", "data", "facebook.bin")
 LAYOUTS = ["hybrid", "uint", "bs", "pshort"]
 
 
@@ -98,8 +96,8 @@ def test_directed_from_csr_rejects_bad_rows(eh):
         eh.HostGraph.directed_from_csr(np.array([0, 1, 1], np.uint64), np.array([5], np.uint32))
 
 
-@pytest.mark.skipif(not os.path.exists(DFB), reason="reference tree not present")
-def test_dfacebook_read_write_bytes(eh):
+def test_dfacebook_read_write_bytes(eh, tmp_path):
+    DFB = _golden.fixture_graph("dfacebook.bin", tmp_path)
     g = eh.HostGraph.read_directed_binary(DFB)
     with tempfile.TemporaryDirectory() as td:
         p = os.path.join(td, "d.bin")
@@ -108,8 +106,9 @@ def test_dfacebook_read_write_bytes(eh):
             assert a.read() == b.read()
 
 
-@pytest.mark.skipif(not os.path.exists(DFB), reason="reference tree not present")
-def test_oracle_gtest_goldens(oracle):
+def test_oracle_gtest_goldens(oracle, tmp_path):
+    DFB = _golden.fixture_graph("dfacebook.bin", tmp_path)
+    FB = _golden.fixture_graph("facebook.bin", tmp_path)
     want = _golden.load_directed()["reference_gtest_goldens"]
     oo, on, io, inn, _ = oracle.read_directed_binary(DFB)
     rows, cols = _oracle_pair(oracle, (oo, on, io, inn), "hybrid")

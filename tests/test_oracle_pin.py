@@ -1,28 +1,25 @@
 """Pins the C oracle to the reference.
 
-1. The reference's own gtest goldens on test/data/facebook.bin
+1. The reference's own gtest goldens on its test/data/facebook.bin
    (test/undirected_triangle_counting_test.cpp:6-13, test/n_clique_test.cpp:6-12,
-   test/undirected_lollipop_counting_test.cpp:6-13, test/similar_nodes_test.cpp:6-13),
-   when the reference tree is present (it is read, never copied).
+   test/undirected_lollipop_counting_test.cpp:6-13, test/similar_nodes_test.cpp:6-13);
+   the graph file is committed as tests/golden/facebook.bin.gz.
 2. Counts and encoded rows produced by the reference binaries themselves on the
    seeded generator graphs (tests/golden/reference_counts.json, made by
    tests/golden/make_golden.py from oracle/build_ref.sh builds).
 """
 import hashlib
-import os
 
 import pytest
 
 import _golden
 
-FB = os.path.join(_golden.REFERENCE_TREE, "test", "data", "facebook.bin")
 LAYOUTS = ["hybrid", "uint", "bs", "pshort"]
 
 
-@pytest.mark.skipif(not os.path.exists(FB), reason="reference tree not present")
 @pytest.mark.parametrize("layout", LAYOUTS + ["hybrid3"])
-def test_facebook_gtest_goldens(oracle, layout):
-    off, nbr, _ = oracle.read_binary(FB)
+def test_facebook_gtest_goldens(oracle, layout, tmp_path):
+    off, nbr, _ = oracle.read_binary(_golden.fixture_graph("facebook.bin", tmp_path))
     want = _golden.load()["reference_gtest_goldens"]
     got = oracle.counts(off, nbr, layout)
     for k in ("triangles", "cliques4", "lollipops", "similar_nodes"):
