@@ -13,9 +13,11 @@ the reference's own "Time[UNDIRECTED TRIANGLE COUNTING]" timer measures).
 `e2e` runs the same pass through the C ABI from pinned host CSR buffers: upload,
 device select/optimize/encode, count, and the u64 result copied back.
 
---impl reference times the reference's algorithm on the host cores instead (the
-C oracle port; the reference's own sources use x86 SSE/AVX and do not build on
-the aarch64 host of the GPU machine).
+--impl reference times the reference's algorithm on the host cores instead: the
+C oracle port (oracle/eh_oracle.c) over the same graph, regenerated on the CPU by
+oracle/eh_gen.c (the GPU library is not loaded), the whole graph counted in
+every step.  The reference's own sources use x86 SSE/AVX and do not build on the
+aarch64 host of the GPU machine.
 
 Multi-GPU: every rank counts its own replica of the graph (the count does not
 need an exchange); value = total edges over all ranks / slowest rank's time.
@@ -49,7 +51,7 @@ def parse_args():
                         "--scale 16 --edges 1000000 --seed 1 --layout uint)")
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--layout", default="hybrid")
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile", action="store_true", help="minimal run for ncu captures")
@@ -90,14 +92,42 @@ def edge_count(a):
     return a.edges if a.edges else a.edge_factor << a.scale
 
 
-def workload(a):
+def workload(a, world=1):
+    """The config object, identical for both arms of the same run."""
     size = ("%d edges" % a.edges) if a.edges else ("edge factor %d" % a.edge_factor)
     return {
         "workload": "undirected triangle count, R-MAT scale %d %s (a=.57,b=.19,c=.19), "
                     "seed %d, %s layout, degree-ordered, nbr<node pruning" % (a.scale, size, a.seed, a.layout),
         "graph": "rmat", "scale": a.scale, "undirected_edges": edge_count(a), "seed": a.seed,
         "layout": a.layout,
+        "l2": "GPU: a 256 MiB L2 flush is written before every timed step (and the encoded rows are larger "
+              "than the 129 MB L2 at scale 22)",
+        "parallelism": "replicas" if world > 1 else "single GPU",
     }
+
+
+def fixture_counts():
+    """Reference-binary counts of the benchmark graphs (tests/golden/reference_large.json),
+    keyed by graph name, with the CSR SHA-256 they were made on."""
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "reference_large.json")) as f:
+            return {g["name"]: g for g in json.load(f)["graphs"]}
+    except (OSError, ValueError, KeyError):
+        return {}
+
+
+def fixture_for(a):
+    name = "rmat_s%d_ef%d_seed%d" % (a.scale, edge_count(a) >> a.scale, a.seed)
+    g = fixture_counts().get(name)
+    return g if g and g["params"]["edges"] == edge_count(a) else None
+
+
+def csr_sha(off, nbr):
+    import hashlib
+    h = hashlib.sha256()
+    h.update(off.astype("<u8").tobytes())
+    h.update(nbr.astype("<u4").tobytes())
+    return h.hexdigest()
 
 
 def measured_peak():
@@ -220,32 +250,43 @@ def cpu_count(off, nbr, layout, max_seconds=20.0):
 
 
 def run_reference(a, rank, world):
-    work = workload(a)
+    """The reference's triangle count (the C oracle port of apps/
+    undirected_triangle_counting.cpp, OpenMP over all host cores) on the whole
+    graph in every step.  The graph comes from oracle/eh_gen.c, the CPU copy of
+    the library's generator, and is checked against the reference-binary
+    fixture's CSR SHA-256 and count when one exists for the configuration."""
+    work = workload(a, world)
     if rank != 0:
         return
-    off, nbr = make_graph(a)
     from oracle import oracle as O
+    t = time.perf_counter()
+    off, nbr = O.rmat_graph(a.scale, edge_count(a), a.seed)
+    t_gen = time.perf_counter() - t
+    fx = fixture_for(a)
+    if fx and csr_sha(off, nbr) != fx["csr_sha256"]:
+        raise SystemExit("regenerated graph differs from the fixture graph %s" % fx["name"])
+    t = time.perf_counter()
     m = O.Matrix(off, nbr, O.SELECT_LOWER, O.LAYOUTS[a.layout])
+    t_build = time.perf_counter() - t
     _, cards, _ = m.row_meta()
     threads = O.lib().oracle_max_threads()
-    total_edges = float(cards.sum())
-    n = len(off) - 1
-    # Size each step: full graph if one pass takes <= 10 s, else a prefix of rows.
-    t = time.perf_counter()
-    m.triangles_range(0, n // 64)
-    est = (time.perf_counter() - t) * 64
-    hi = n if est <= 10.0 else max(1, int(n * 10.0 / est))
-    edges = float(cards[:hi].sum())
+    edges = float(cards.sum())
+    count = None
     for _ in range(a.warmup):
-        m.triangles_range(0, hi)
+        count = m.triangles()
     times = []
     for _ in range(a.steps):
         t = time.perf_counter()
-        m.triangles_range(0, hi)
+        c = m.triangles()
         times.append(time.perf_counter() - t)
+        if count is not None and c != count:
+            raise SystemExit("nondeterministic CPU count: %d vs %d" % (c, count))
+        count = c
+    if fx and count != fx["counts"]["triangles"]:
+        raise SystemExit("CPU count %d differs from the reference binary's %d" % (count, fx["counts"]["triangles"]))
     ms = 1e3 * statistics.mean(times)
     value = edges / (ms / 1e3)
-    sample = "full graph per step" if hi == n else "rows [0, %d) of %d per step" % (hi, n)
+    sample = "full graph per step (%d pruned edges), mean of %d steps" % (edges, len(times))
     out = {
         "impl": "reference", "metric": "triangle-count edges/s (pruned undirected edges per second)",
         "value": value, "unit": "edges/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -255,7 +296,9 @@ def run_reference(a, rank, world):
                          "cpu": cpu_model(),
                          "sample": sample + "; C oracle port of the reference algorithm (OpenMP)"},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "pruned_edges_total": total_edges,
+        "count": count,
+        "count_matches_reference_binary": (count == fx["counts"]["triangles"]) if fx else None,
+        "setup_s": {"generate": t_gen, "build": t_build},
     }
     print(json.dumps(out), flush=True)
 
@@ -268,7 +311,7 @@ def run_ours(a, rank, world, local_rank):
     if dist:
         import torch.distributed as tdist
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    work = workload(a)
+    work = workload(a, world)
     L = eh.load()
     off, nbr = make_graph(a)
     stream = torch.cuda.current_stream()
@@ -317,6 +360,10 @@ def run_ours(a, rank, world, local_rank):
     count = int(out.item())
     if count != count_ref:
         raise SystemExit("nondeterministic count: %d vs %d" % (count, count_ref))
+    fx0 = fixture_for(a)
+    if fx0 and count != fx0["counts"]["triangles"]:
+        raise SystemExit("GPU count %d differs from the reference binary's %d on %s"
+                         % (count, fx0["counts"]["triangles"], fx0["name"]))
     value, ms_max = aggregate(pruned, ms, world, "cuda")
 
     # End to end through the C ABI from pinned host buffers.
@@ -353,12 +400,12 @@ def run_ours(a, rank, world, local_rank):
             tdist.destroy_process_group()
         return
     peak, peak_kind = measured_peak()
-    achieved = btc / (ms / 1e3) / 1e9
     # A count launches the heavy-pivot kernel when some row is longer than the
     # light-pivot limit and the light-pivot kernel when some row is not.
     light_max = (shape or {}).get("light_max", 96)
     kernels_per_count = 1 + (info["max_row_cardinality"] > light_max)
     traffic = traffic_per_launch(work)
+    fx = fixture_for(a)
     cpu = None
     if not a.no_cpu and not a.profile and world == 1:
         v, dt, threads, sample, ccount, tb = cpu_count(off, nbr, a.layout)
@@ -366,29 +413,38 @@ def run_ours(a, rank, world, local_rank):
                "sample": sample +
                "; C oracle port of the reference algorithm (OpenMP, build %.2f s untimed)" % tb,
                "count_matches_gpu": (ccount == count) if ccount is not None else None}
+    # Roofline: the physical HBM figure is the count's DRAM traffic (ncu, the
+    # two pivot kernels of one count) over the event-timed count.  The survey's
+    # algorithmic bytes B_tc charge every neighbour row in full per edge while
+    # the kernels probe words of it (much of it from L2), so B_tc / time is an
+    # effective bandwidth above what HBM can deliver, reported beside it.
+    algo_gbs = btc / (ms / 1e3) / 1e9
+    dram_gbs = (traffic / (ms / 1e3) / 1e9) if traffic else None
+    roofline = {"bound": "hbm", "achieved": dram_gbs, "peak": peak, "unit": "GB/s",
+                "frac": (dram_gbs / peak) if dram_gbs else None, "traffic": traffic, "peak_kind": peak_kind,
+                "achieved_basis": "ncu DRAM bytes (read + write) of one count's kernels / CUDA-event count time",
+                "nominal_gbs": NOMINAL_HBM_GBS,
+                "frac_of_nominal": (dram_gbs / NOMINAL_HBM_GBS) if dram_gbs else None,
+                "algorithmic_bytes_per_launch": btc,
+                "algorithmic_formula": "sum_i [8 + bytes(A_i)] + sum_{(i,j) in E<} bytes(B_j), bytes = layout "
+                                       "payload (every neighbour row charged in full per edge)",
+                "effective_gbs": algo_gbs,
+                "effective_note": "algorithmic bytes / count time: an effective bandwidth, not an HBM fraction "
+                                  "(the kernels read words of the rows, many from L2)"}
     res = {
         "metric": "triangle-count edges/s (pruned undirected edges per second)",
         "value": value, "unit": "edges/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (seeded R-MAT generator)",
-        "config": dict(work, l2="256 MiB L2 flush written before every timed step; encoded rows "
-                                "%.0f MB %s 129 MB L2" % (info["row_total_bytes_used"] / 1e6,
-                                                          ">" if info["row_total_bytes_used"] > 129e6 else "<"),
-                       parallelism="replicas" if world > 1 else "single GPU", work_shape=shape),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "nominal_gbs": NOMINAL_HBM_GBS, "frac_of_nominal": achieved / NOMINAL_HBM_GBS,
-                     "algorithmic_bytes_per_launch": btc,
-                     "formula": "sum_i [8 + bytes(A_i)] + sum_{(i,j) in E<} bytes(B_j), bytes = layout payload",
-                     "dram_gbs": (traffic / (ms / 1e3) / 1e9) if traffic else None,
-                     "dram_frac": (traffic / (ms / 1e3) / 1e9 / peak) if traffic else None,
-                     "note": "one count = the heavy-pivot and light-pivot kernels; traffic is their ncu DRAM "
-                             "bytes per count, dram_gbs that over the event-timed count"},
+        "config": work,
+        "work_shape": shape,
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks,
         "gpu_launches": a.steps * kernels_per_count,
         "count": count,
+        "count_matches_reference_binary": (count == fx["counts"]["triangles"]) if fx else None,
         "wall_s_timed_region": wall,
         "graph": {"vertices": info["matrix_size"], "pruned_edges": pruned,
                   "bitset_rows": info["num_bitset_rows"], "uint_rows": info["num_uint_rows"],
@@ -444,6 +500,15 @@ def run_cliques(a):
         tl = _events_ms(lambda: full.count_lollipops_async(out.data_ptr(), stream.cuda_stream), stream, a.steps, flush)
         res.update({"cliques4": c4, "cliques4_ms": statistics.median(t4[a.warmup:] or t4),
                     "lollipops": lp, "lollipops_ms": statistics.median(tl[a.warmup:] or tl)})
+        fx = fixture_counts().get(name)
+        if fx and a.layout in ("hybrid", "uint", "bs", "pshort", "hybrid3"):
+            if csr_sha(off, nbr) != fx["csr_sha256"]:
+                raise SystemExit("generated graph differs from the fixture graph %s" % name)
+            res["cliques4_matches_reference_binary"] = c4 == fx["counts"]["cliques4"]
+            res["lollipops_match_reference_binary"] = lp == fx["counts"]["lollipops"]
+            if c4 != fx["counts"]["cliques4"] or lp != fx["counts"]["lollipops"]:
+                print(json.dumps(res), flush=True)
+                raise SystemExit("count differs from the reference binary on %s" % name)
         if not a.no_cpu:
             t = time.perf_counter()
             om = O.Matrix(off, nbr, O.SELECT_LOWER, O.LAYOUTS[a.layout])
@@ -555,11 +620,22 @@ def run_batch(a):
     per_ms = statistics.median(ptimes)
     same = pt.cpu().tolist() == bt and pc.cpu().tolist() == bc
     edges = info["cardinality"]
+    fx = None
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "reference_large.json")) as f:
+            fx = json.load(f)["batch"]
+    except (OSError, ValueError, KeyError):
+        pass
+    ref_match = None
+    if fx and G <= fx["num_graphs"]:
+        ref_match = bt == fx["triangles"][:G] and bc == fx["cliques4"][:G]
+        if not ref_match:
+            raise SystemExit("batched counts differ from the reference binaries' per-graph counts")
     print(json.dumps({
         "workload": "batch", "metric": "graphs counted per second (triangles + 4-cliques)", "unit": "graphs/s",
         "value": G / (batched_ms / 1e3), "higher_is_better": True, "n_graphs": G,
         "batched_ms": batched_ms, "per_graph_launch_ms": per_ms, "speedup_vs_per_graph": per_ms / batched_ms,
-        "counts_identical": same, "pruned_edges": edges, "edges_per_s": edges / (batched_ms / 1e3),
+        "counts_identical": same, "counts_match_reference_binary": ref_match, "pruned_edges": edges, "edges_per_s": edges / (batched_ms / 1e3),
         "total_triangles": int(sum(bt)), "total_cliques4": int(sum(bc)), "tuned_shape": shape,
         "generation_s": t_gen, "data": "synthetic (seeded G(n,M) / Barabasi-Albert generators)",
         "cuda_graph_replay": True}), flush=True)

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
-SRC = os.path.join(HERE, "eh_oracle.c")
+SRC = [os.path.join(HERE, "eh_oracle.c"), os.path.join(HERE, "eh_gen.c")]
 
 # Layout and selection codes shared with the engine (common::type values).
 BITSET, PSHORT, UINTEGER, HYBRID, HYBRID3 = 0, 1, 2, 5, 16
@@ -25,10 +25,11 @@ SELECTIONS = {"all": SELECT_ALL, "lower": SELECT_LOWER, "mask": SELECT_MASK}
 def build(force=False):
     """Compiles the oracle with the host gcc (no GPU needed)."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB_PATH) and \
+            all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in SRC):
         return LIB_PATH
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-fopenmp", "-o", tmp, SRC])
+    subprocess.check_call(["gcc", "-O3", "-std=gnu99", "-fPIC", "-shared", "-fopenmp", "-o", tmp, *SRC])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -70,6 +71,10 @@ def lib():
         L.oracle_n_path.argtypes = [P, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint64)]
         L.oracle_list_triangles.restype = C.c_uint64
         L.oracle_list_triangles.argtypes = [P, P, C.c_uint64]
+        L.oracle_rmat.restype = C.c_uint64
+        L.oracle_rmat.argtypes = [C.c_uint32, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                  C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+        L.oracle_gen_free.argtypes = [P]
         _lib = L
     return _lib
 
@@ -164,6 +169,20 @@ class Matrix:
         out = np.zeros(len(a), np.uint32)
         lib().oracle_intersect_rows(self.h, _ptr(a), _ptr(b), len(a), _ptr(out), self.threads)
         return out
+
+
+def rmat_graph(scale, edges, seed, a=0.57, b=0.19, c=0.19):
+    """(offsets, nbrs) of the library's seeded R-MAT graph, degree-ordered,
+    regenerated on the CPU by oracle/eh_gen.c (same CSR, byte for byte)."""
+    po, pn = C.c_void_p(), C.c_void_p()
+    n = int(lib().oracle_rmat(scale, edges, a, b, c, seed, C.byref(po), C.byref(pn)))
+    if n == 0:
+        raise RuntimeError("R-MAT scale %d could not reach %d distinct edges" % (scale, edges))
+    off = np.ctypeslib.as_array(C.cast(po, C.POINTER(C.c_uint64)), (n + 1,)).copy()
+    nbr = np.ctypeslib.as_array(C.cast(pn, C.POINTER(C.c_uint32)), (int(off[n]),)).copy()
+    lib().oracle_gen_free(po)
+    lib().oracle_gen_free(pn)
+    return off, nbr
 
 
 def read_binary(path):

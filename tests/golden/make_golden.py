@@ -11,8 +11,13 @@ the reference's binary format, and records:
     (x86-64 or aarch64) can prove it got the same input.
 With --directed it writes tests/golden/reference_directed.json instead: the
 symbiosity and n_path apps on seeded directed graphs (directed binary format).
+With --large it writes tests/golden/reference_large.json: the reference
+binaries' counts on the benchmark-size graphs (R-MAT scale 22 edge factor 16
+triangles; R-MAT scale 20 and the planted-clique graph on 2^20 vertices,
+4-cliques and lollipops) and on every graph of the 4,096-graph batch
+(triangles and 4-cliques), each keyed by the SHA-256 of the generated CSR.
 Needs an x86-64 host with the reference tree (the reference uses SSE/AVX).
-Usage: python tests/golden/make_golden.py [--directed]
+Usage: python tests/golden/make_golden.py [--directed | --large]
 """
 import hashlib
 import json
@@ -176,12 +181,110 @@ def main_directed():
     print("wrote", OUT_DIRECTED)
 
 
+OUT_LARGE = os.path.join(HERE, "reference_large.json")
+
+# Benchmark-size graphs: (name, how to generate, apps).  Counts do not depend on
+# the layout (the reference's own cross-layout agreement), so the reference
+# runs the hybrid layout, the one these workloads use.
+LARGE = [
+    {"name": "rmat_s22_ef16_seed2", "kind": "rmat", "seed": 2, "params": {"scale": 22, "edges": 16 << 22},
+     "apps": ["triangles"]},
+    {"name": "rmat_s20_ef16_seed3", "kind": "rmat", "seed": 3, "params": {"scale": 20, "edges": 16 << 20},
+     "apps": ["triangles", "cliques4", "lollipops"]},
+    {"name": "planted_2^20_p1e-4_1024cliques_seed3", "kind": "planted_workload", "seed": 3, "params": {},
+     "apps": ["triangles", "cliques4", "lollipops"]},
+]
+
+
+def large_graph(spec):
+    if spec["kind"] == "planted_workload":
+        from simdgraphprocessing_gb300 import workloads as W
+        return W.planted_graph(spec["seed"])
+    return eh.graph(spec["kind"], spec["seed"], **spec["params"])
+
+
+def run_app_threads(binary, graph, layout, threads):
+    return subprocess.run([os.path.join(REF, binary), "--graph=" + graph, "--input_type=binary",
+                           "--t=%d" % threads, "--layout=" + layout], stdout=subprocess.PIPE,
+                          stderr=subprocess.STDOUT, text=True, check=True).stdout
+
+
+def batch_reference_counts(td, threads):
+    """The reference's triangle and 4-clique counts of every graph of the
+    4,096-graph batch workload (seeds 4 + k), in batch order."""
+    import concurrent.futures as cf
+    from simdgraphprocessing_gb300 import workloads as W
+    specs = W.batch_specs()
+    h = hashlib.sha256()
+    tri, clq = [0] * len(specs), [0] * len(specs)
+
+    def one(k):
+        kind, s, kw = specs[k]
+        g = eh.graph(kind, s, **kw)
+        path = os.path.join(td, "batch_%d.bin" % k)
+        g.write_binary(path)
+        t = int(re.search(APPS["triangles"][1], run_app_threads("undirected_triangle_counting", path, "hybrid",
+                                                                1)).group(1))
+        c = int(re.search(APPS["cliques4"][1], run_app_threads("n_clique", path, "hybrid", 1)).group(1))
+        os.unlink(path)
+        off, nbr, _, _ = g.csr()
+        return k, t, c, csr_sha(off, nbr)
+
+    shas = [None] * len(specs)
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        for k, t, c, sha in ex.map(one, range(len(specs))):
+            tri[k], clq[k], shas[k] = t, c, sha
+            if k % 256 == 0:
+                print("batch", k, t, c, flush=True)
+    for sha in shas:
+        h.update(bytes.fromhex(sha))
+    return {"num_graphs": len(specs), "seed": 4, "layout": "hybrid",
+            "csr_sha256_of_shas": h.hexdigest(), "triangles": tri, "cliques4": clq,
+            "total_triangles": sum(tri), "total_cliques4": sum(clq)}
+
+
+def main_large():
+    threads = os.cpu_count() or 4
+    entries = []
+    with tempfile.TemporaryDirectory(dir=os.environ.get("EH_GOLDEN_TMP")) as td:
+        for spec in LARGE:
+            g = large_graph(spec)
+            off, nbr, _, _ = g.csr()
+            path = os.path.join(td, spec["name"] + ".bin")
+            g.write_binary(path)
+            e = dict(spec)
+            e["n"] = int(len(off) - 1)
+            e["directed_edges"] = int(len(nbr))
+            e["csr_sha256"] = csr_sha(off, nbr)
+            del g, off, nbr
+            e["counts"] = {}
+            for key in spec["apps"]:
+                binary, pat = APPS[key]
+                out = run_app_threads(binary, path, "hybrid", threads)
+                e["counts"][key] = int(re.search(pat, out).group(1))
+                print(spec["name"], key, e["counts"][key], flush=True)
+            os.unlink(path)
+            entries.append(e)
+        batch = batch_reference_counts(td, threads)
+    doc = {
+        "generated_by": "tests/golden/make_golden.py --large",
+        "reference_binaries": "oracle/build_ref.sh (unmodified reference sources), hybrid layout",
+        "graphs": entries,
+        "batch": batch,
+    }
+    with open(OUT_LARGE, "w") as f:
+        json.dump(doc, f, indent=1, sort_keys=True)
+    print("wrote", OUT_LARGE)
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "ref_rowdump")):
-        sys.exit("oracle/_ref is not built; run: sh oracle/build_ref.sh /root/reference")
+        sys.exit("oracle/_ref is not built; run: sh oracle/build_ref.sh <reference tree>")
     eh.load()
     if "--directed" in sys.argv:
         return main_directed()
+    if "--large" in sys.argv:
+        return main_large()
     entries = []
     with tempfile.TemporaryDirectory() as td:
         for spec in GRAPHS:
