@@ -86,6 +86,30 @@ cudaError_t upload_stream(cudaStream_t* out) {
   return cudaSuccess;
 }
 
+void note_use(Matrix* m, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+  std::lock_guard<std::mutex> g(m->uses_mu);
+  cudaEvent_t ev = nullptr;
+  for (auto& u : m->uses)
+    if (u.first == st) ev = u.second;
+  if (!ev) {
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return;
+    m->uses.emplace_back(st, ev);
+  }
+  cudaEventRecord(ev, st);
+}
+
+cudaError_t wait_uses(Matrix* m, cudaStream_t st) {
+  std::lock_guard<std::mutex> g(m->uses_mu);
+  for (auto& u : m->uses) {
+    if (u.first == st) continue;  // stream order covers it
+    const cudaError_t e = cudaStreamWaitEvent(st, u.second, 0);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr, const uint8_t* d_mask,
                        int sel, int layout, cudaStream_t st, Matrix** out, uint64_t total, const UploadChunks* up) {
   EH_CHECK_ARG(out != nullptr, "out is NULL");
@@ -126,10 +150,10 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
   };
   auto fail = [&](eh_status s) {
     cleanup();
+    cudaFreeAsync(m->desc, st);
+    cudaFreeAsync(m->arena, st);
+    cudaFreeAsync(m->counters, st);
     cudaStreamSynchronize(st);
-    cudaFree(m->desc);
-    cudaFree(m->arena);
-    cudaFree(m->counters);
     delete m;
     return s;
   };
@@ -195,9 +219,9 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
     return fail(cuda_fail(e, "encode kernel"));
   cleanup();
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
-    cudaFree(m->desc);
-    cudaFree(m->arena);
-    cudaFree(m->counters);
+    cudaFreeAsync(m->desc, st);
+    cudaFreeAsync(m->arena, st);
+    cudaFreeAsync(m->counters, st);
     delete m;
     return cuda_fail(e, "encode");
   }
@@ -229,9 +253,9 @@ eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaSt
     n_units = last_start + last_cnt;
   }
   if (!p.units || p.units_cap < (uint64_t)n_units) {
-    if (p.units) {
-      CU(cudaDeviceSynchronize(), "units");  // launches on other streams may still read them
-      cudaFree(p.units);
+    if (p.units) {  // launches on other streams may still read them
+      CU(wait_uses(m, st), "units");
+      CU(cudaFreeAsync(p.units, st), "units");
       m->device_bytes -= p.units_cap * sizeof(uint2);
     }
     p.units_cap = n_units ? n_units : 1;
@@ -257,9 +281,9 @@ eh_status ensure_core(Matrix* m, cudaStream_t st) {
   uint32_t want = (uint32_t)std::min<uint64_t>(m->n, m->core_limit) & ~63u;
   if (m->n < 4096) want = 0;
   if (want == p.core_k && (want == 0 || p.core)) return EH_OK;
-  if (p.core) {
-    CU(cudaDeviceSynchronize(), "core");  // launches on other streams may still read it
-    cudaFree(p.core);
+  if (p.core) {  // launches on other streams may still read it
+    CU(wait_uses(m, st), "core");
+    CU(cudaFreeAsync(p.core, st), "core");
     m->device_bytes -= core_row_offset(p.core_k) * 8;
     p.core = nullptr;
     p.core_k = 0;
@@ -305,12 +329,20 @@ eh_status ensure_plan(Matrix* m, cudaStream_t st) {
     std::vector<uint32_t> dec_rows;
     std::vector<unsigned long long> dec_off;
     if (p.n_giant) {
+      // The giant rows' ids and descriptors come back in one synchronisation:
+      // a gather kernel collects their descriptors next to each other first.
+      std::vector<RowDesc> gdesc(p.n_giant);
+      RowDesc* d_gdesc = nullptr;
+      CU(pool_alloc((void**)&d_gdesc, p.n_giant * sizeof(RowDesc), st), "giant scratch");
+      CU(launch_gather_desc(m->desc, p.order, p.n_giant, d_gdesc, st), "giant gather");
       CU(cudaMemcpyAsync(grows.data(), p.order, p.n_giant * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
          "giant copy");
+      CU(cudaMemcpyAsync(gdesc.data(), d_gdesc, p.n_giant * sizeof(RowDesc), cudaMemcpyDeviceToHost, st),
+         "giant desc");
+      cudaFreeAsync(d_gdesc, st);
       CU(cudaStreamSynchronize(st), "giant");
       for (uint32_t u = 0; u < p.n_giant; u++) {
-        RowDesc d;
-        CU(cudaMemcpy(&d, m->desc + grows[u], sizeof(RowDesc), cudaMemcpyDeviceToHost), "giant desc");
+        const RowDesc& d = gdesc[u];
         if (desc_type(d) != TY_UINT) {
           goff[u] = gtotal;
           dec_rows.push_back(grows[u]);
@@ -362,6 +394,7 @@ PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
   a.num_graphs = 0;
   a.core = m->plan.core;
   a.core_k = m->plan.core_k;
+  a.core_hot_words = m->core_hot_words;
   return a;
 }
 
@@ -420,11 +453,13 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
         grid = (int)std::min<uint64_t>(grid, w.clique_scratch_words / slot);
         if (grid < 1) return set_error(EH_ERR_OUT_OF_MEMORY, "workspace too small for a %u-entry pivot", cmax);
       } else {
-        cudaStreamSynchronize(st);
-        cudaFree(m->clique_scratch);
+        if (m->clique_scratch) {  // earlier launches on any stream may still use it
+          CU(wait_uses(m, st), "clique scratch");
+          CU(cudaFreeAsync(m->clique_scratch, st), "clique scratch");
+        }
         m->clique_scratch = nullptr;
         m->clique_scratch_words = 0;
-        CU(cudaMalloc((void**)&m->clique_scratch, slot * grid * 4), "clique scratch allocation");
+        CU(pool_alloc((void**)&m->clique_scratch, slot * grid * 4, st), "clique scratch allocation");
         m->clique_scratch_words = slot * grid;
         w.clique_scratch = m->clique_scratch;
         w.clique_scratch_words = m->clique_scratch_words;
@@ -449,6 +484,7 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
     const int grid = (int)std::min<uint64_t>((nL - nB + 63) / 64, 8ull * sms);
     CU(launch_clique_light(a, nB, nL, w.counters + 11, grid > 0 ? grid : 1, st), "clique kernel (warp)");
   }
+  note_use(m, st);
   return EH_OK;
 }
 
@@ -457,6 +493,7 @@ eh_status launch_lollipop_count(Matrix* m, unsigned long long* out, cudaStream_t
   if (s != EH_OK) return s;
   PivotArgs a = pivot_args(m, out);
   CU(launch_lollipops(a, m->plan.units, m->plan.n_units, m->grid, st), "lollipop kernel");
+  note_use(m, st);
   return EH_OK;
 }
 
@@ -471,6 +508,7 @@ eh_status launch_triangle_count(Matrix* m, unsigned long long* out, const uint32
   a.graph_rows = graph_rows;
   a.num_graphs = num_graphs;
   CU(launch_triangles(a, m->plan.units, m->plan.n_units, m->grid, st), "triangle kernel");
+  note_use(m, st);
   return EH_OK;
 }
 
@@ -705,18 +743,19 @@ void eh_matrix_free(eh_matrix_t mh) {
   Matrix* m = MX(mh);
   if (!m) return;
   cudaSetDevice(m->device);
-  // cudaFree does not wait for the device on stream-ordered (pool) memory:
-  // let every launch that may still read the matrix finish first.
-  cudaDeviceSynchronize();
-  cudaFree(m->desc);
-  cudaFree(m->arena);
-  cudaFree(m->counters);
-  cudaFree(m->plan.order);
-  cudaFree(m->plan.units);
-  cudaFree(m->plan.giant_lists);
-  cudaFree(m->plan.giant_off);
-  cudaFree(m->plan.core);
-  cudaFree(m->clique_scratch);
+  // The buffers go back to the pool on the library's upload stream once every
+  // launch recorded on the matrix (on any stream) has finished; neither the
+  // host nor other streams wait.
+  cudaStream_t st = nullptr;
+  if (eh::upload_stream(&st) != cudaSuccess || eh::wait_uses(m, st) != cudaSuccess) {
+    cudaDeviceSynchronize();  // no stream to order the frees on: fall back to waiting here
+    st = nullptr;
+  }
+  void* bufs[] = {m->desc, m->arena, m->counters, m->plan.order, m->plan.units, m->plan.giant_lists,
+                  m->plan.giant_off, m->plan.core, m->clique_scratch};
+  for (void* b : bufs)
+    if (b) cudaFreeAsync(b, st);
+  for (auto& u : m->uses) cudaEventDestroy(u.second);
   delete m;
 }
 
@@ -758,6 +797,7 @@ eh_status eh_similar_nodes_async(eh_matrix_t mh, uint32_t threshold, uint64_t* d
   CU(eh::launch_similar(m->n, m->desc, m->arena, vstar, threshold, reinterpret_cast<unsigned long long*>(d_count),
                         ST(stream)),
      "similar_nodes kernel");
+  eh::note_use(m, ST(stream));
   return EH_OK;
 }
 
@@ -775,6 +815,7 @@ eh_status eh_intersect_rows(eh_matrix_t mh, const uint32_t* d_a, const uint32_t*
   EH_CHECK_ARG(npairs == 0 || (d_a && d_b && d_counts), "NULL pair arrays");
   Matrix* m = MX(mh);
   CU(eh::launch_intersect_rows(m->n, m->desc, m->arena, d_a, d_b, npairs, d_counts, ST(stream)), "intersect kernel");
+  eh::note_use(m, ST(stream));
   return EH_OK;
 }
 

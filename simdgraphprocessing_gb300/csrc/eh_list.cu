@@ -161,5 +161,6 @@ extern "C" eh_status eh_list_triangles(eh_matrix_t mh, uint32_t* d_out, uint64_t
     k_list_warp<<<(unsigned)std::min<uint64_t>((p.n_order - n_large + 7) / 8, 8ull * sms), kCtaThreads, 0, st>>>(
         a, n_large, p.n_order);
   e = cudaGetLastError();
+  note_use(m, st);
   return e == cudaSuccess ? EH_OK : set_error(EH_ERR_CUDA, "listing kernels: %s", cudaGetErrorString(e));
 }

@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -66,15 +68,21 @@ struct Matrix {
   uint32_t light_max = kDefaultLightMax;
   uint32_t unit_span = kDefaultUnitSpan;
   uint32_t core_limit = kCoreDefaultK;  // rows in the dense core at most (0 = no core)
+  uint32_t core_hot_words = 0;          // see PivotArgs::core_hot_words
   bool is_batch = false;            // the union matrix of an eh_batch_t
+  // Where the matrix's buffers are read: one event per stream, recorded after
+  // every launch that reads them (not while that stream is being captured).
+  // Freeing or replacing a buffer makes the freeing stream wait for these
+  // events, not for the whole device.
+  std::mutex uses_mu;
+  std::vector<std::pair<cudaStream_t, cudaEvent_t>> uses;
 };
 
 // eh_capi.cu
 // Stream-ordered allocation (cudaMallocAsync semantics) from the library's own
-// pool on the current device, for scratch (freed with cudaFreeAsync) and for a
-// matrix's buffers (freed with cudaFree after cudaDeviceSynchronize: cudaFree
-// does not wait for the device on pool memory; every build and plan step
-// synchronises its stream before other streams use them).
+// pool on the current device, for scratch and for a matrix's buffers, all freed
+// with cudaFreeAsync: scratch on the stream that used it, a matrix's buffers on
+// a stream made to wait for the matrix's recorded uses (note_use / wait_uses).
 // The pool keeps up to kPoolKeep bytes of freed memory mapped between calls:
 // the device's default pool releases it at every synchronisation, and mapping
 // 400 MB again costs about 1 ms on GB300.
@@ -101,6 +109,10 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
 eh_status ensure_plan(Matrix* m, cudaStream_t st);
 eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaStream_t st);
 eh_status ensure_core(Matrix* m, cudaStream_t st);
+// Records that launches reading m's buffers were just queued on st.
+void note_use(Matrix* m, cudaStream_t st);
+// Makes st wait for every launch note_use has recorded on m, on any stream.
+cudaError_t wait_uses(Matrix* m, cudaStream_t st);
 // eh_batch.cu: tuned work shape of this matrix's size class, if the tuner has one.
 void apply_cached_shape(Matrix* m);
 PivotArgs pivot_args(Matrix* m, unsigned long long* out);

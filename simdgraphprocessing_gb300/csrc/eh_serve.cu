@@ -4,12 +4,24 @@
 //
 // A dispatcher thread owns `slots` CUDA streams, each with its own workspace
 // (work-queue counters, clique scratch slots, pinned result word).  Queries
-// wait in a FIFO; whenever a slot is free and the query's scratch fits under
-// the HBM cap (resident graphs + scratch held by slots), the query is launched
-// on that slot at once, so queries that arrive while others run overlap with
-// them on the device.  Completion is detected by polling each slot's event
-// (cudaEventQuery, never a blocking wait), and callers wait on their ticket
-// with a timeout.
+// wait in arrival order; whenever a slot is free and a query's scratch fits
+// under the HBM cap (resident graphs + scratch held by slots), the query is
+// launched on that slot at once, so queries that arrive while others run
+// overlap with them on the device.  A query whose scratch does not fit yet
+// waits while younger queries that fit pass it, at most kMaxBypass of them;
+// then admission stops until it has started (a bounded wait for large
+// queries, no head-of-line blocking for small ones).  A query that fills the
+// GPU by itself (a triangle or clique count on a graph of at least
+// kFillEdges pruned edges) runs only while no other such query does: two of
+// them side by side are slower than one after the other (they compete for
+// the SMs and thrash each other's rows in L2), while small queries fit in
+// beside one.  Such a query waiting for the running one lets younger small
+// queries pass without limit (it starts as soon as the running one ends) and
+// keeps its place ahead of younger large ones.  Slot scratch comes from
+// the library's stream-ordered pool on the slot's own stream (no device-wide
+// synchronisation while other slots run).  Completion is detected by polling
+// each slot's event (cudaEventQuery, never a blocking wait), and callers wait
+// on their ticket with a timeout.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -51,6 +63,7 @@ struct Slot {
   uint64_t* h_out = nullptr;  // pinned: [0] the count, [1] the query's device error flags
   uint64_t ticket = 0;
   bool busy = false;
+  bool fills = false;  // the running query fills the GPU by itself
 };
 
 struct GraphEntry {
@@ -61,6 +74,10 @@ struct GraphEntry {
 };
 
 }  // namespace
+
+constexpr uint32_t kMaxBypass = 64;     // younger queries that may pass a waiting one
+constexpr uint64_t kFillEdges = 8ull << 20;  // pruned edges from which a count fills the GPU
+constexpr size_t kAdmissionWindow = 256;  // queued queries looked at per admission round
 
 struct Server {
   int device = 0;
@@ -74,6 +91,8 @@ struct Server {
   std::unordered_map<uint64_t, Query> queries;
   uint64_t next_ticket = 1;
   uint64_t completed = 0, launched = 0, max_inflight = 0;
+  uint64_t blocked_ticket = 0;  // oldest query waiting for memory, and how often it has been passed
+  uint32_t bypassed = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   bool stop = false;
@@ -90,6 +109,11 @@ uint64_t query_scratch_words(const GraphEntry& ge, uint32_t kind, uint32_t k, in
   if (!nG) return 0;
   const uint64_t grid = std::min<uint64_t>(nG, 2ull * sms);
   return clique_slot_words((uint32_t)m->tot.max_card, k) * grid;
+}
+
+// Whether query q alone keeps every SM busy for its whole run.
+bool fills_gpu(const Server* s, const Query& q) {
+  return q.kind != EH_QUERY_SIMILAR_NODES && s->graphs[q.graph].low->tot.cardinality >= kFillEdges;
 }
 
 eh_status launch_query(Server* s, Slot& sl, const Query& q) {
@@ -140,49 +164,86 @@ void dispatch_loop(Server* s) {
       progress = true;
     }
     if (progress) s->cv_done.notify_all();
-    // Admission: free slot + memory under the cap, FIFO order.
-    for (uint32_t i = 0; i < s->nslots && !s->queue.empty(); i++) {
-      Slot& sl = s->slots[i];
-      if (sl.busy) continue;
-      const uint64_t ticket = s->queue.front();
+    // Admission, oldest first: each queued query takes a free slot when its
+    // scratch fits under the cap; one that does not fit lets younger queries
+    // pass (at most kMaxBypass in all) while slots drain and free memory.
+    size_t qi = 0;
+    bool blocked = false;
+    bool filling = false;  // a GPU-filling query is running, or the oldest waiting one is
+    for (const Slot& o : s->slots) filling = filling || (o.busy && o.fills);
+    while (qi < s->queue.size() && qi < kAdmissionWindow) {
+      int free_slot = -1;
+      const uint64_t ticket = s->queue[qi];
       Query& q = s->queries[ticket];
+      const bool fills = fills_gpu(s, q);
+      if (fills && filling) {  // waits for the running one; smaller queries go ahead
+        filling = true;
+        qi++;
+        continue;
+      }
       const uint64_t need = query_scratch_words(s->graphs[q.graph], q.kind, q.param, sms);
+      for (uint32_t i = 0; i < s->nslots; i++) {  // a free slot, preferring one whose scratch already fits
+        if (s->slots[i].busy) continue;
+        if (free_slot < 0 || (s->slots[i].ws.clique_scratch_words >= need &&
+                              s->slots[free_slot].ws.clique_scratch_words < need))
+          free_slot = (int)i;
+      }
+      if (free_slot < 0) break;
+      Slot& sl = s->slots[free_slot];
       if (need > sl.ws.clique_scratch_words) {
         const uint64_t grow = (need - sl.ws.clique_scratch_words) * 4;
         if (s->resident + s->scratch + grow > s->cap) {
-          if (inflight == 0 && s->scratch > 0) {
-            // Nothing running: give back idle slots' scratch before waiting for it.
-            for (Slot& o : s->slots)
-              if (!o.busy && o.ws.clique_scratch) {
-                cudaFree(o.ws.clique_scratch);
-                s->scratch -= o.ws.clique_scratch_words * 4;
-                o.ws.clique_scratch = nullptr;
-                o.ws.clique_scratch_words = 0;
-              }
-            if (s->resident + need * 4 > s->cap) {  // can never fit
-              s->queue.pop_front();
-              q.status = set_error(EH_ERR_ADMISSION, "query needs %llu scratch bytes above the HBM cap",
-                                   (unsigned long long)(need * 4));
-              q.done = true;
-              q.done_ns = now_ns();
-              s->cv_done.notify_all();
-              progress = true;
+          // Idle slots give their scratch back (stream-ordered, nothing waits).
+          for (Slot& o : s->slots)
+            if (!o.busy && &o != &sl && o.ws.clique_scratch) {
+              cudaFreeAsync(o.ws.clique_scratch, o.st);
+              s->scratch -= o.ws.clique_scratch_words * 4;
+              o.ws.clique_scratch = nullptr;
+              o.ws.clique_scratch_words = 0;
+            }
+        }
+        if (s->resident + s->scratch + grow > s->cap) {
+          if (s->resident + need * 4 > s->cap) {  // can never fit
+            s->queue.erase(s->queue.begin() + qi);
+            q.status = set_error(EH_ERR_ADMISSION, "query needs %llu scratch bytes above the HBM cap",
+                                 (unsigned long long)(need * 4));
+            q.done = true;
+            q.done_ns = now_ns();
+            s->cv_done.notify_all();
+            progress = true;
+            continue;
+          }
+          if (!blocked) {  // the oldest query waiting for memory
+            blocked = true;
+            if (s->blocked_ticket != ticket) {
+              s->blocked_ticket = ticket;
+              s->bypassed = 0;
             }
           }
-          break;  // FIFO: wait for memory
+          if (s->bypassed >= kMaxBypass) break;  // it has waited long enough: no more passing
+          qi++;
+          continue;
         }
-        cudaFree(sl.ws.clique_scratch);
-        s->scratch -= sl.ws.clique_scratch_words * 4;
-        sl.ws.clique_scratch = nullptr;
-        sl.ws.clique_scratch_words = 0;
-        if (cudaMalloc((void**)&sl.ws.clique_scratch, need * 4) != cudaSuccess) break;
+        if (sl.ws.clique_scratch) {
+          cudaFreeAsync(sl.ws.clique_scratch, sl.st);
+          s->scratch -= sl.ws.clique_scratch_words * 4;
+          sl.ws.clique_scratch = nullptr;
+          sl.ws.clique_scratch_words = 0;
+        }
+        if (pool_alloc((void**)&sl.ws.clique_scratch, need * 4, sl.st) != cudaSuccess) {
+          sl.ws.clique_scratch = nullptr;
+          break;  // retried on the next round, when other slots may have released memory
+        }
         sl.ws.clique_scratch_words = need;
         s->scratch += need * 4;
       }
-      s->queue.pop_front();
+      s->queue.erase(s->queue.begin() + qi);
+      if (blocked) s->bypassed++;
       q.start_ns = now_ns();
-      q.slot = (int32_t)i;
+      q.slot = free_slot;
       sl.ticket = ticket;
+      sl.fills = fills;
+      filling = filling || fills;
       const eh_status st = launch_query(s, sl, q);
       if (st != EH_OK) {
         q.status = st;
@@ -367,7 +428,7 @@ void eh_server_free(eh_server_t sh) {
     if (sl.ev) cudaEventDestroy(sl.ev);
     if (sl.st) cudaStreamDestroy(sl.st);
     cudaFree(sl.ws.counters);
-    cudaFree(sl.ws.clique_scratch);
+    if (sl.ws.clique_scratch) cudaFreeAsync(sl.ws.clique_scratch, nullptr);
     cudaFree(sl.d_out);
     if (sl.h_out) cudaFreeHost(sl.h_out);
   }

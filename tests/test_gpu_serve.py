@@ -60,3 +60,70 @@ def test_admission_and_bounded_waits(eh):
     with pytest.raises(eh.EHError):
         srv.submit(99, eh.QUERY_TRIANGLES)
     srv.close()
+
+
+def _complete_graph(n):
+    off = np.arange(0, n * n, n - 1, dtype=np.uint64)[: n + 1]
+    nbr = np.array([u for v in range(n) for u in range(n) if u != v], np.uint32)
+    return off, nbr
+
+
+def test_memory_blocked_query_lets_small_queries_pass(eh):
+    """A 4-clique query whose pivots need global scratch waits while another
+    such query holds the memory under the cap; small queries submitted after
+    it start before it (bounded bypass, no head-of-line blocking); a query that
+    can never fit is refused; every answer equals the query run alone."""
+    big_g = _complete_graph(1900)  # pivots of up to 1,899 entries: above the shared-memory tier
+    small_g = eh.graph("rmat", 6, scale=10, edges=6000).csr()[:2]
+    probe = eh.Server(slots=2, hbm_cap_bytes=8 << 30)
+    b0, s0 = probe.add_graph(*big_g), probe.add_graph(*small_g)
+    probe.wait(probe.submit(b0, eh.QUERY_CLIQUES, 4))
+    st = probe.stats()
+    need, resident = st["scratch_bytes"], st["resident_bytes"]
+    want_big = probe.run_alone(b0, eh.QUERY_CLIQUES, 4)
+    want_small = probe.run_alone(s0, eh.QUERY_TRIANGLES)
+    probe.close()
+    assert need > 0 and want_big == 1900 * 1899 * 1898 * 1897 // 24
+
+    srv = eh.Server(slots=6, hbm_cap_bytes=resident + need + need // 2)  # room for one big query's scratch
+    b, s = srv.add_graph(*big_g), srv.add_graph(*small_g)
+    first = srv.submit(b, eh.QUERY_CLIQUES, 4)
+    second = srv.submit(b, eh.QUERY_CLIQUES, 4)
+    smalls = [srv.submit(s, eh.QUERY_TRIANGLES) for _ in range(12)]
+    r1, r2 = srv.wait(first), srv.wait(second)
+    rs = [srv.wait(t) for t in smalls]
+    assert r1["count"] == r2["count"] == want_big
+    assert all(r["count"] == want_small and r["status"] == 0 for r in rs)
+    assert r2["start_ns"] >= r1["done_ns"]  # the two big queries never held scratch at once
+    assert any(r["start_ns"] < r2["start_ns"] for r in rs)  # smaller queries passed the waiting one
+    srv.close()
+
+    tight = eh.Server(slots=2, hbm_cap_bytes=resident + need // 2)
+    b, s = tight.add_graph(*big_g), tight.add_graph(*small_g)
+    t_big, t_small = tight.submit(b, eh.QUERY_CLIQUES, 4), tight.submit(s, eh.QUERY_TRIANGLES)
+    with pytest.raises(eh.EHError) as e:
+        tight.wait(t_big)
+    assert e.value.status == 8  # EH_ERR_ADMISSION: its scratch can never fit under the cap
+    assert tight.wait(t_small)["count"] == want_small
+    tight.close()
+
+
+def test_gpu_filling_queries_run_one_at_a_time(eh):
+    """Counts on a graph of at least 8M pruned edges fill the GPU by themselves:
+    the server runs them one after another (never side by side), while a small
+    query submitted after them starts before the last of them; every answer
+    equals the query run alone."""
+    big_g = eh.graph("rmat", 31, scale=19, edges=9 << 20).csr()[:2]
+    small_g = eh.graph("rmat", 32, scale=10, edges=6000).csr()[:2]
+    srv = eh.Server(slots=4, hbm_cap_bytes=32 << 30)
+    b, s = srv.add_graph(*big_g), srv.add_graph(*small_g)
+    want_big, want_small = srv.run_alone(b, eh.QUERY_TRIANGLES), srv.run_alone(s, eh.QUERY_TRIANGLES)
+    bigs = [srv.submit(b, eh.QUERY_TRIANGLES) for _ in range(3)]
+    small = srv.submit(s, eh.QUERY_TRIANGLES)
+    rb = [srv.wait(t) for t in bigs]
+    rs = srv.wait(small)
+    srv.close()
+    assert all(r["count"] == want_big for r in rb) and rs["count"] == want_small
+    for x, y in zip(rb, rb[1:]):
+        assert y["start_ns"] >= x["done_ns"]  # in submission order, never overlapping
+    assert rs["start_ns"] < rb[-1]["start_ns"]  # the small query did not wait behind them
