@@ -224,8 +224,13 @@ eh_status eh_count_cliques_async(eh_matrix_t m, uint32_t k, uint64_t* d_count, v
  * rejected with EH_ERR_UNSUPPORTED.  The matrix must already have its work plan
  * (made by its first eh_count_* call), else EH_ERR_INVALID_ARGUMENT.  The first
  * call on a device looks up the array's address (cudaGetSymbolAddress) and
- * should come before any stream capture.  All calls share the array: calls
- * whose kernels overlap on the GPU race. */
+ * should come before any stream capture; the address is kept for the life of
+ * the process, so the device must not be reset (cudaDeviceReset) after that
+ * first call.  All calls share the array: calls whose kernels overlap on the
+ * GPU race.  It runs the shared-memory tier as one launch sized for its
+ * largest pivot (eh_count_cliques splits it into size bands), so on skewed
+ * graphs it can be slower than eh_count_cliques.  eh_matrix_free does not wait
+ * for these launches: synchronize their stream before freeing the matrix. */
 eh_status eh_count_cliques_noalloc(eh_matrix_t m, uint32_t k, uint64_t* d_count, void* stream);
 /* undirected_lollipop_counting<T,R>::run (apps/undirected_lollipop_counting.cpp:27-77).
  * Matrix built with EH_SELECT_ALL. */
@@ -280,6 +285,9 @@ typedef struct eh_tuning {
   uint32_t core_rows;     /* highest-degree rows kept as a dense bitmap (0 = none)   */
   float ms;               /* median triangle-count time with the chosen shape        */
   uint32_t configs_tried;
+  uint32_t core_hot_words; /* light-pivot probes of the first words of each dense-core
+                              row keep their L2 lines, the rest are evicted first
+                              (0 = no cache hints)                                  */
 } eh_tuning;
 /* Times the triangle count (EH_SELECT_LOWER) or the lollipop count
  * (EH_SELECT_ALL) on this matrix for a small set of work shapes, coordinate by
@@ -287,6 +295,12 @@ typedef struct eh_tuning {
  * layout, selection, size bucket) in the process (and in the file named by
  * EH_TUNE_CACHE, if set). */
 eh_status eh_matrix_tune(eh_matrix_t m, void* stream, eh_tuning* result);
+/* Uses the given work shape (light_max, unit_span, ctas_per_sm, core_rows,
+ * core_hot_words of `shape`; ms and configs_tried are ignored) for this
+ * matrix's later counts, rebuilding its plan as needed.  Counts do not depend
+ * on the shape.  EH_ERR_INVALID_ARGUMENT for a value outside the tuner's
+ * ranges.  (No reference counterpart.) */
+eh_status eh_matrix_set_shape(eh_matrix_t m, const eh_tuning* shape, void* stream);
 
 /* ------------------------------------------------------------------------- */
 /* Batches: many graphs counted in one launch (no reference counterpart; each   */

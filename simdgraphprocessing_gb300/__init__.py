@@ -34,7 +34,8 @@ class EHError(RuntimeError):
 
 class Tuning(C.Structure):
     _fields_ = [("light_max", C.c_uint32), ("unit_span", C.c_uint32), ("ctas_per_sm", C.c_uint32),
-                ("core_rows", C.c_uint32), ("ms", C.c_float), ("configs_tried", C.c_uint32)]
+                ("core_rows", C.c_uint32), ("ms", C.c_float), ("configs_tried", C.c_uint32),
+                ("core_hot_words", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):
@@ -129,6 +130,7 @@ def load(build_if_missing=True):
         "eh_selftest_bounded_wait": (I, [U32, C.POINTER(U32)]),
         "eh_list_triangles": (I, [P, P, U64, P, P]),
         "eh_matrix_tune": (I, [P, P, C.POINTER(Tuning)]),
+        "eh_matrix_set_shape": (I, [P, C.POINTER(Tuning), P]),
         "eh_batch_build": (I, [U32, P, U64, P, P, I, P, C.POINTER(P)]),
         "eh_batch_count": (I, [P, U32, P, P]),
         "eh_batch_run": (I, [P, P, P, I, P]),
@@ -439,6 +441,12 @@ class Matrix:
         t = Tuning()
         check(load().eh_matrix_tune(self.h, _stream(stream), C.byref(t)))
         return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
+    def set_shape(self, light_max, unit_span, ctas_per_sm, core_rows, core_hot_words=0, stream=None):
+        """Uses this work shape for later counts (eh_matrix_set_shape)."""
+        t = Tuning(light_max=light_max, unit_span=unit_span, ctas_per_sm=ctas_per_sm, core_rows=core_rows,
+                   core_hot_words=core_hot_words)
+        check(load().eh_matrix_set_shape(self.h, C.byref(t), _stream(stream)))
 
     def intersect_rows(self, d_a, d_b, npairs, d_counts, stream=None):
         check(load().eh_intersect_rows(self.h, C.c_void_p(d_a), C.c_void_p(d_b), npairs,

@@ -44,7 +44,7 @@ struct Batch {
 namespace {
 
 struct Shape {
-  uint32_t light_max, unit_span, ctas, core;
+  uint32_t light_max, unit_span, ctas, core, hot;
 };
 
 std::mutex g_tune_mutex;
@@ -73,9 +73,13 @@ void load_tune_file() {
   if (!path) return;
   FILE* f = fopen(path, "r");
   if (!f) return;
-  char key[512];
-  unsigned lm, us, ct, co;
-  while (fscanf(f, "%511s %u %u %u %u", key, &lm, &us, &ct, &co) == 5) g_tune_cache[key] = Shape{lm, us, ct, co};
+  char line[1024];
+  while (fgets(line, sizeof(line), f)) {  // key light_max unit_span ctas core [hot]
+    char key[512];
+    unsigned lm, us, ct, co, hot = 0;
+    if (sscanf(line, "%511s %u %u %u %u %u", key, &lm, &us, &ct, &co, &hot) >= 5)
+      g_tune_cache[key] = Shape{lm, us, ct, co, hot};
+  }
   fclose(f);
 }
 
@@ -85,7 +89,7 @@ void store_tune(const std::string& key, const Shape& s) {
   if (!path) return;
   FILE* f = fopen(path, "a");
   if (!f) return;
-  fprintf(f, "%s %u %u %u %u\n", key.c_str(), s.light_max, s.unit_span, s.ctas, s.core);
+  fprintf(f, "%s %u %u %u %u %u\n", key.c_str(), s.light_max, s.unit_span, s.ctas, s.core, s.hot);
   fclose(f);
 }
 
@@ -101,6 +105,7 @@ eh_status apply_shape(Matrix* m, const Shape& s, cudaStream_t st) {
   m->light_max = s.light_max;
   m->unit_span = s.unit_span;
   m->core_limit = s.core;
+  m->core_hot_words = s.hot;
   m->grid = sms * (int)s.ctas;
   return ensure_plan(m, st);
 }
@@ -143,10 +148,10 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
   const std::string key = tune_key(m, graph_rows != nullptr);
   unsigned long long* out = nullptr;
   const size_t outn = graph_rows ? num_graphs : 1;
-  if (cudaMalloc((void**)&out, outn * sizeof(unsigned long long)) != cudaSuccess)
+  if (pool_alloc((void**)&out, outn * sizeof(unsigned long long), st) != cudaSuccess)
     return set_error(EH_ERR_OUT_OF_MEMORY, "tuner output allocation failed");
   auto it = g_tune_cache.find(key);
-  Shape best{m->light_max, m->unit_span, (uint32_t)max_ctas_per_sm(m->device), m->core_limit};
+  Shape best{m->light_max, m->unit_span, (uint32_t)max_ctas_per_sm(m->device), m->core_limit, m->core_hot_words};
   float best_ms = 0;
   uint32_t tried = 0;
   if (it != g_tune_cache.end()) {
@@ -172,24 +177,29 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
     };
     const Shape start = best;
     for (uint32_t co : {0u, 16384u, 32768u, 65536u, 98304u, 131072u})
-      if (co != start.core && co <= kCoreMaxK) consider(Shape{start.light_max, start.unit_span, start.ctas, co});
+      if (co != start.core && co <= kCoreMaxK) consider(Shape{start.light_max, start.unit_span, start.ctas, co, start.hot});
+    const Shape after_core0 = best;
+    if (after_core0.core)
+      for (uint32_t hot : {0u, 32u, 64u, 128u})
+        if (hot != after_core0.hot)
+          consider(Shape{after_core0.light_max, after_core0.unit_span, after_core0.ctas, after_core0.core, hot});
     const Shape after_core = best;
     for (int c = 1; c <= cmax; c++)
       if ((uint32_t)c != after_core.ctas)
-        consider(Shape{after_core.light_max, after_core.unit_span, (uint32_t)c, after_core.core});
+        consider(Shape{after_core.light_max, after_core.unit_span, (uint32_t)c, after_core.core, after_core.hot});
     const Shape after_ctas = best;
     for (uint32_t lm : {32u, 64u, 96u})
       if (lm != after_ctas.light_max && lm <= kLightMax)
-        consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas, after_ctas.core});
+        consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas, after_ctas.core, after_ctas.hot});
     const Shape after_lm = best;
     for (uint32_t us : {32u, 128u, 256u, 512u, 1024u, 2048u})
-      if (us != after_lm.unit_span) consider(Shape{after_lm.light_max, us, after_lm.ctas, after_lm.core});
+      if (us != after_lm.unit_span) consider(Shape{after_lm.light_max, us, after_lm.ctas, after_lm.core, after_lm.hot});
     if (s == EH_OK) {
       s = apply_shape(m, best, st);
       store_tune(key, best);
     }
   }
-  cudaFree(out);
+  cudaFreeAsync(out, st);
   if (s != EH_OK) return s;
   if (res) {
     res->light_max = best.light_max;
@@ -198,6 +208,7 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
     res->core_rows = best.core;
     res->ms = best_ms;
     res->configs_tried = tried;
+    res->core_hot_words = best.hot;
   }
   return EH_OK;
 }
@@ -216,6 +227,7 @@ void apply_cached_shape(Matrix* m) {
   m->light_max = it->second.light_max;
   m->unit_span = it->second.unit_span;
   m->core_limit = it->second.core;
+  m->core_hot_words = it->second.hot;
   m->grid = sms * (int)it->second.ctas;
 }
 
@@ -234,6 +246,21 @@ eh_status eh_matrix_tune(eh_matrix_t mh, void* stream, eh_tuning* result) {
     return set_error(EH_ERR_UNSUPPORTED,
                      "tuning times the triangle count (EH_SELECT_LOWER) or the lollipop count (EH_SELECT_ALL)");
   return eh::tune(m, nullptr, 0, reinterpret_cast<cudaStream_t>(stream), result);
+}
+
+eh_status eh_matrix_set_shape(eh_matrix_t mh, const eh_tuning* shape, void* stream) {
+  EH_CHECK_ARG(mh && shape, "NULL argument");
+  eh::Matrix* m = reinterpret_cast<eh::Matrix*>(mh);
+  cudaSetDevice(m->device);
+  EH_CHECK_ARG(shape->light_max >= 2 && shape->light_max <= eh::kLightMax, "light_max %u outside [2, %u]",
+               shape->light_max, eh::kLightMax);
+  EH_CHECK_ARG(shape->unit_span >= 1 && shape->unit_span <= 65536, "unit_span %u outside [1, 65536]",
+               shape->unit_span);
+  EH_CHECK_ARG(shape->ctas_per_sm >= 1 && (int)shape->ctas_per_sm <= eh::max_ctas_per_sm(m->device),
+               "ctas_per_sm %u outside [1, %d]", shape->ctas_per_sm, eh::max_ctas_per_sm(m->device));
+  EH_CHECK_ARG(shape->core_rows <= eh::kCoreMaxK, "core_rows %u above %u", shape->core_rows, eh::kCoreMaxK);
+  const eh::Shape s{shape->light_max, shape->unit_span, shape->ctas_per_sm, shape->core_rows, shape->core_hot_words};
+  return eh::apply_shape(m, s, reinterpret_cast<cudaStream_t>(stream));
 }
 
 eh_status eh_batch_build(uint32_t num_graphs, const uint64_t* graph_rows, uint64_t n, const uint64_t* offsets,
@@ -267,13 +294,18 @@ eh_status eh_batch_build(uint32_t num_graphs, const uint64_t* graph_rows, uint64
   b->num_graphs = num_graphs;
   std::vector<uint32_t> gr(num_graphs + 1);
   for (uint32_t g = 0; g <= num_graphs; g++) gr[g] = (uint32_t)graph_rows[g];
-  if (cudaMalloc((void**)&b->d_graph_rows, gr.size() * 4) != cudaSuccess) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (eh::pool_alloc((void**)&b->d_graph_rows, gr.size() * 4, st) != cudaSuccess) {
     eh_matrix_free(mh);
     delete b;
     return set_error(EH_ERR_OUT_OF_MEMORY, "batch allocation failed");
   }
-  cudaMemcpy(b->d_graph_rows, gr.data(), gr.size() * 4, cudaMemcpyHostToDevice);
-  s = eh::ensure_plan(b->m, reinterpret_cast<cudaStream_t>(stream));
+  if (cudaMemcpyAsync(b->d_graph_rows, gr.data(), gr.size() * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    eh_batch_free(reinterpret_cast<eh_batch_t>(b));
+    return set_error(EH_ERR_CUDA, "batch graph boundaries upload failed");
+  }
+  s = eh::ensure_plan(b->m, st);
   if (s != EH_OK) {
     eh_batch_free(reinterpret_cast<eh_batch_t>(b));
     return s;
@@ -336,6 +368,7 @@ eh_status eh_batch_run(eh_batch_t bh, uint64_t* d_triangles, uint64_t* d_cliques
     b->exec_clq = d_cliques4;
   }
   const cudaError_t e = cudaGraphLaunch(b->exec, st);
+  eh::note_use(b->m, st);
   return e == cudaSuccess ? EH_OK : set_error(EH_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
 }
 
@@ -355,7 +388,17 @@ void eh_batch_free(eh_batch_t bh) {
   if (!b) return;
   cudaSetDevice(b->m->device);
   if (b->exec) cudaGraphExecDestroy(b->exec);
-  cudaFree(b->d_graph_rows);
+  // The graph boundaries go back to the pool once the matrix's recorded
+  // launches are done (they read them), like the matrix's own buffers.
+  cudaStream_t st = nullptr;
+  if (b->d_graph_rows) {
+    if (eh::upload_stream(&st) == cudaSuccess && eh::wait_uses(b->m, st) == cudaSuccess) {
+      cudaFreeAsync(b->d_graph_rows, st);
+    } else {
+      cudaDeviceSynchronize();
+      cudaFreeAsync(b->d_graph_rows, nullptr);
+    }
+  }
   eh_matrix_free(reinterpret_cast<eh_matrix_t>(b->m));
   delete b;
 }

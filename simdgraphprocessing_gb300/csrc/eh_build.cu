@@ -611,6 +611,13 @@ __global__ void k_plan_scatter(uint64_t n, const RowDesc* __restrict__ desc, uin
 }
 
 // Decodes whole rows into plain sorted u32 lists (one block per row).
+// out[u] = desc[rows[u]]: the descriptors of a list of rows, for one copy to the host.
+__global__ void k_gather_desc(const RowDesc* __restrict__ desc, const uint32_t* __restrict__ rows, uint32_t nrows,
+                              RowDesc* __restrict__ out) {
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u < nrows) out[u] = desc[rows[u]];
+}
+
 __global__ void k_decode_rows(const RowDesc* __restrict__ desc, const uint4* __restrict__ arena,
                               const uint32_t* __restrict__ rows,
                               const unsigned long long* __restrict__ dst_off, uint32_t* __restrict__ dst) {
@@ -752,6 +759,13 @@ cudaError_t launch_plan(uint64_t n, const RowDesc* desc, uint32_t min_card, uint
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint64_t n, uint32_t* out, uint32_t* tmp,
                                cudaStream_t st) {
   return exclusive_scan(Plain{in}, n, out, tmp, st);
+}
+
+cudaError_t launch_gather_desc(const RowDesc* desc, const uint32_t* rows, uint32_t nrows, RowDesc* out,
+                               cudaStream_t st) {
+  if (nrows == 0) return cudaSuccess;
+  k_gather_desc<<<(nrows + 255) / 256, 256, 0, st>>>(desc, rows, nrows, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_decode_rows(const RowDesc* desc, const uint4* arena, const uint32_t* rows,

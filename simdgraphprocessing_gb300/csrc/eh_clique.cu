@@ -43,7 +43,8 @@ __device__ __forceinline__ uint32_t ilog2p1_c(uint32_t x) { return 32u - __clz(x
 // lengths of rows 0 .. e-1.  A c-entry pivot needs mask_off(c) words, about
 // half of a c x c bit matrix.
 __host__ __device__ __forceinline__ uint32_t mask_len(uint32_t e) { return ((e + 31) >> 5) | 1u; }
-// 32-bit arithmetic: exact for e < 65,536 (mask_off(65535) < 2^27).
+// 32-bit arithmetic: exact below kCliqueMaxPivot = 2^18 entries, the largest
+// pivot a clique count accepts (mask_off(2^18 - 1) = 1,073,987,583 < 2^32).
 __host__ __device__ __forceinline__ uint32_t mask_off(uint32_t e) {
   if (e == 0) return 0;
   const uint32_t A = (e - 1) >> 5, r = (e - 1) & 31;

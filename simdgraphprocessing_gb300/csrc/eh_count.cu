@@ -75,23 +75,23 @@ __device__ uint32_t pair_count_warp(const uint32_t* L, uint32_t e, const RowView
     const uint32_t lo = max(A.aux, B.aux);
     const uint32_t hi = min(min(A.aux + A.len, B.aux + B.len), (j >> 6) + 1);
     if (hi <= lo) return 0;
-    if (hi - lo <= 2 * e) {
-      const unsigned long long* wa = static_cast<const unsigned long long*>(A.p);
-      const unsigned long long* wb = static_cast<const unsigned long long*>(B.p);
-      const unsigned long long last_mask = (1ull << (j & 63)) - 1ull;
-      for (uint32_t w = lo + lane; w < hi; w += 32) {
-        unsigned long long x = wa[w - A.aux] & wb[w - B.aux];
-        if (w == (j >> 6)) x &= last_mask;
-        c += __popcll(x);
-      }
+    if (hi - lo <= 2 * e) {  // 128-bit AND + popcount over the overlapping words below j
+      c = bitset_and_lane(A.p, A.aux, B.p, B.aux, B.len, lo, hi, j >> 6, (1ull << (j & 63)) - 1ull, lane);
       return warp_sum_u32(c);
     }
   }
   // Probe cost: e lookups into B.  Stream cost: |B| lookups into the pivot.
+  // Merge cost (uint rows): e + |B| steps of a merge path.
   bool stream = false;
   if (B.type == TY_UINT) {
     const uint32_t look = (A.type == TY_BITSET) ? 1u : ilog2p1(e);
-    stream = (uint64_t)B.card * look < (uint64_t)e * ilog2p1(B.card) * 4u;
+    const uint64_t probe_cost = (uint64_t)e * ilog2p1(B.card) * 4u, stream_cost = (uint64_t)B.card * look;
+    if (A.type != TY_BITSET && e >= 64 && (uint64_t)e + B.card < min(probe_cost, stream_cost)) {
+      const uint32_t* b = static_cast<const uint32_t*>(B.p);
+      const uint32_t nb = lower_bound_u32(b, 0, B.card, j);  // full rows hold elements >= j too
+      return warp_sum_u32(merge_path_lane(L, e, b, nb, lane));
+    }
+    stream = stream_cost < probe_cost;
   } else if (B.type == TY_PSHORT) {
     stream = (uint64_t)B.card * ilog2p1(e) < (uint64_t)e * (B.aux + ilog2p1(B.card)) * 4u;
   }
@@ -123,6 +123,37 @@ __device__ __forceinline__ uint32_t pair_count_stream(const uint32_t* L, uint32_
     });
   }
   return c;
+}
+
+// |{t < e : L[t] in row(j)}| for j in the dense core, by one lane.  Core row
+// j holds row(j) ∩ [0, j) as bits: AND it with the pivot's staged bits when j
+// is within them and that takes no more steps (ceil(wj / 2) 128-bit word
+// pairs) than probing it at the e pivot elements below j, else probe.  (At
+// R-MAT scale 22, 29.6 M pairs AND and 5.6 M probe; streaming row(j) into the
+// pivot instead would be cheaper for none of them.)
+__device__ __forceinline__ uint32_t core_pair_lane(const PivotArgs& a, const uint32_t* L, uint32_t e, uint32_t j,
+                                                   uint32_t and_k, const unsigned long long* abits) {
+  const unsigned long long* row = a.core + core_row_offset(j);
+  const uint32_t np = (((j + 63) >> 6) + 1) >> 1;
+  uint32_t cnt = 0;
+  if (j <= and_k && np <= e) {
+    // The core row starts 16-byte aligned and ends in a zero pad word; the
+    // staged bits are 16-byte aligned.
+    const uint4* r4 = reinterpret_cast<const uint4*>(row);
+    const uint4* b4 = reinterpret_cast<const uint4*>(abits);
+#pragma unroll 1
+    for (uint32_t q = 0; q < np; q++) {
+      const uint4 x = b4[q], y = __ldg(r4 + q);
+      cnt += __popcll(lo64(x) & lo64(y)) + __popcll(hi64(x) & hi64(y));
+    }
+    return cnt;
+  }
+#pragma unroll 1
+  for (uint32_t t = 0; t < e; t++) {
+    const uint32_t x = L[t];
+    cnt += (uint32_t)((__ldg(row + (x >> 6)) >> (x & 63)) & 1ull);
+  }
+  return cnt;
 }
 
 // Heavy pivots: 6 resident CTAs per SM, 40 registers per thread (the per-pair
@@ -189,44 +220,34 @@ __global__ void __launch_bounds__(kCtaThreads, 6) k_pivots_heavy(PivotArgs a, co
     const uint32_t e0 = 1 + uu.y * a.unit_span;
     const uint32_t e1 = min(c, e0 + a.unit_span);
     unsigned long long uacc = 0;
-    for (uint32_t e = e0 + warp; e < e1; e += NWARPS) {
-      const uint32_t j = L[e];
-      uint32_t cnt;
-      if (use_core && j < a.core_k) {
-        // Core row j holds row(j) ∩ [0, j).  Cheapest of: AND it with the pivot's
-        // bits (j within the staged bits; wj words), probe it at the e pivot
-        // elements below j (e words), or stream row(j) itself and look each
-        // element up in the pivot (|row(j)| lookups; rows past the highest-degree
-        // ones are short while e grows with the pivot).
-        const unsigned long long* row = a.core + core_row_offset(j);
-        const uint32_t wj = (j + 63) >> 6;
-        cnt = 0;
-        if (j <= and_k && wj <= e) {
-          for (uint32_t w = lane; w < wj; w += 32) cnt += __popcll(s.abits[w] & __ldg(row + w));
+    // Pairs (i, j = L[e]) with j in the dense core run one per lane: the lane
+    // does the pair's whole AND or probe loop, so the per-pair work (core row
+    // offset, choice, reduction) is paid once per 32 pairs instead of once per
+    // pair.  Pairs outside the core are collected by ballot and intersected by
+    // the whole warp, each with its own layout pair.
+    for (uint32_t base = e0 + 32 * warp; base < e1; base += kCtaThreads) {
+      const uint32_t e = base + lane;
+      uint32_t j = 0;
+      bool coop = false;
+      if (e < e1) {
+        j = L[e];
+        if (use_core && j < a.core_k) {
+          const uint32_t cnt = core_pair_lane(a, L, e, j, and_k, s.abits);
+          uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
         } else {
-          bool stream = false;
-          RowView B;
-          if (e > kStreamMinE) {
-            B = load_view(a.desc, a.arena, j);
-            stream = (uint64_t)B.card * (A.type == TY_BITSET ? 1u : ilog2p1(e)) < e;
-          }
-          if (stream) {
-            cnt = pair_count_stream(L, e, A, B, j, lane);
-          } else {
-            for (uint32_t t = lane; t < e; t += 32) {
-              const uint32_t x = L[t];
-              cnt += (uint32_t)((__ldg(row + (x >> 6)) >> (x & 63)) & 1ull);
-            }
-          }
+          coop = true;
         }
-        cnt = warp_sum_u32(cnt);
-      } else {
-        const RowView B = load_view(a.desc, a.arena, j);
-        cnt = pair_count_warp(L, e, A, B, j, lane);
       }
-      if (lane == 0) uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+      for (uint32_t pend = __ballot_sync(FULL, coop); pend; pend &= pend - 1) {
+        const uint32_t src = __ffs(pend) - 1;
+        const uint32_t jj = __shfl_sync(FULL, j, src);
+        const RowView B = load_view(a.desc, a.arena, jj);
+        const uint32_t cnt = pair_count_warp(L, base + src, A, B, jj, lane);
+        if (lane == 0) uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+      }
     }
     if (a.graph_rows) {  // batch: this unit's count goes to its graph
+      uacc = warp_sum_u64(uacc);
       if (lane == 0 && uacc) atomicAdd(&a.out[graph_of(a.graph_rows, a.num_graphs, i)], uacc);
     } else {
       acc += uacc;
@@ -266,8 +287,14 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
       uint32_t cnt = 0;
       for (uint32_t q = lane; q < pairs; q += 32) {
         const uint32_t j = list[e], x = list[t];
-        if (j < a.core_k) {  // x < j: one word of the L2-resident core
-          cnt += (uint32_t)((__ldg(a.core + core_row_offset(j) + (x >> 6)) >> (x & 63)) & 1ull);
+        if (j < a.core_k) {  // x < j: one word of the core row j
+          // With core_hot_words set, words near the start of each core row
+          // (the highest-degree columns, where most probes land) keep their L2
+          // lines and the others are evicted first.
+          const unsigned long long* p = a.core + core_row_offset(j) + (x >> 6);
+          const uint32_t hot = a.core_hot_words;
+          const unsigned long long w = hot == 0 ? __ldg(p) : (x >> 6) < hot ? ld_keep(p) : ld_stream(p);
+          cnt += (uint32_t)((w >> (x & 63)) & 1ull);
         } else {
           const RowView B = load_view(a.desc, a.arena, j);
           cnt += row_contains(B, x);
@@ -297,7 +324,7 @@ __global__ void __launch_bounds__(256) k_core_build(const RowDesc* __restrict__ 
   for (uint32_t j = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); j < core_k; j += nw) {
     unsigned long long* row = core + core_row_offset(j);
     const uint32_t wj = (j + 63) >> 6;
-    for (uint32_t w = lane; w < wj; w += 32) row[w] = 0ull;
+    for (uint32_t w = lane; w < core_row_words(j); w += 32) row[w] = 0ull;  // with the pad word
     __syncwarp();
     const RowView B = load_view(desc, arena, j);
     if (B.type == TY_BITSET) {
@@ -336,13 +363,14 @@ __global__ void k_unit_fill(const uint32_t* __restrict__ cnt, const uint32_t* __
 __global__ void __launch_bounds__(256) k_similar(uint64_t n, const RowDesc* __restrict__ desc,
                                                  const uint4* __restrict__ arena, uint32_t vstar,
                                                  uint32_t threshold, unsigned long long* out) {
+  __shared__ PshortHdr s_hdr[8];
   const uint32_t lane = threadIdx.x & 31;
   const RowView A = load_view(desc, arena, vstar);
   unsigned long long acc = 0;
   const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
   for (uint64_t r = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); r < n; r += nw) {
     const RowView B = load_view(desc, arena, (uint32_t)r);
-    const uint32_t c = warp_intersect_size(A, B, lane);
+    const uint32_t c = warp_intersect_size(A, B, lane, &s_hdr[threadIdx.x >> 5]);
     if (lane == 0 && c > threshold) acc++;
   }
   if (lane == 0 && acc) atomicAdd(out, acc);
@@ -355,6 +383,7 @@ __global__ void __launch_bounds__(256) k_intersect_rows(uint64_t n, const RowDes
                                                         const uint32_t* __restrict__ ra,
                                                         const uint32_t* __restrict__ rb, uint64_t np,
                                                         uint32_t* __restrict__ counts) {
+  __shared__ PshortHdr s_hdr[8];
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
   for (uint64_t p = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); p < np; p += nw) {
@@ -362,7 +391,8 @@ __global__ void __launch_bounds__(256) k_intersect_rows(uint64_t n, const RowDes
       if (lane == 0) counts[p] = 0xffffffffu;
       continue;
     }
-    const uint32_t c = warp_intersect_size(load_view(desc, arena, ra[p]), load_view(desc, arena, rb[p]), lane);
+    const uint32_t c = warp_intersect_size(load_view(desc, arena, ra[p]), load_view(desc, arena, rb[p]), lane,
+                                           &s_hdr[threadIdx.x >> 5]);
     if (lane == 0) counts[p] = c;
   }
 }

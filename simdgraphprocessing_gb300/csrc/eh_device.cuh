@@ -88,10 +88,111 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 
+// ---- L2 eviction priority of single loads (createpolicy + L2::cache_hint) ----
+// ld_keep marks the line to be evicted last, ld_stream to be evicted first:
+// probes into a small, hot region keep it in L2 while scattered one-off probes
+// do not displace it.  Read-only data (the non-coherent path).
+__device__ __forceinline__ unsigned long long ld_keep(const unsigned long long* p) {
+  unsigned long long v;
+  asm("{\n .reg .b64 pol;\n createpolicy.fractional.L2::evict_last.b64 pol, 1.0;\n"
+      " ld.global.nc.L2::cache_hint.u64 %0, [%1], pol;\n}"
+      : "=l"(v)
+      : "l"(p));
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_stream(const unsigned long long* p) {
+  unsigned long long v;
+  asm("{\n .reg .b64 pol;\n createpolicy.fractional.L2::evict_first.b64 pol, 1.0;\n"
+      " ld.global.nc.L2::cache_hint.u64 %0, [%1], pol;\n}"
+      : "=l"(v)
+      : "l"(p));
+  return v;
+}
+
 __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t x) { return __reduce_add_sync(FULL, x); }
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x) {
   for (int d = 16; d; d >>= 1) x += __shfl_xor_sync(FULL, x, d);
   return x;
+}
+
+// ---- Bitset words as 16-byte pairs ----
+// Every payload starts on a 16-byte boundary and is zero-padded to a multiple
+// of 16 bytes (in the arena and in shared-memory copies of it), so words
+// (2q, 2q+1) of a bitset row are one aligned 128-bit load for every pair
+// q < ceil(len / 2): the GPU form of the reference's 256-bit AVX loads
+// (intersection.hpp:880-955).
+__device__ __forceinline__ unsigned long long lo64(uint4 v) { return ((unsigned long long)v.y << 32) | v.x; }
+__device__ __forceinline__ unsigned long long hi64(uint4 v) { return ((unsigned long long)v.w << 32) | v.z; }
+// Pair q of a row with np pairs (generic address: global or shared), zero outside [0, np).
+__device__ __forceinline__ uint4 ld_pair(const void* w, int32_t q, int32_t np) {
+  if (q < 0 || q >= np) return make_uint4(0u, 0u, 0u, 0u);
+  return reinterpret_cast<const uint4*>(w)[q];
+}
+
+// Per-lane part of sum over words w in [lo, hi) of popc(A_w & B_w), where A_w
+// is word w - a0 of A's payload (a0 = its first word index) and likewise for
+// B (blen words); word mw (if in range) is ANDed with mmask.  Requires
+// a0 <= lo, b0 <= lo and hi <= b0 + blen, hi <= a0 + A's length.  A is walked
+// in aligned pairs, all inside its payload.  B's pairs line up when b0 - a0 is
+// even (then they are inside its payload too); when it is odd each A pair
+// takes the high word of one B pair and the low word of the next, and the two
+// pair indices are clamped to B's payload: a clamped word lies outside
+// [lo, hi) and is masked off.  Word indices are below 2^26, so 32-bit
+// arithmetic is exact.
+__device__ __forceinline__ uint32_t bitset_and_lane(const void* pa, uint32_t a0, const void* pb, uint32_t b0,
+                                                    uint32_t blen, uint32_t lo, uint32_t hi, uint32_t mw,
+                                                    unsigned long long mmask, uint32_t lane) {
+  const uint4* a4 = reinterpret_cast<const uint4*>(pa);
+  const uint4* b4 = reinterpret_cast<const uint4*>(pb);
+  const int32_t d = (int32_t)b0 - (int32_t)a0;
+  const int32_t q1 = (int32_t)(hi - a0 + 1) >> 1;
+  uint32_t c = 0;
+  for (int32_t q = (int32_t)((lo - a0) >> 1) + (int32_t)lane; q < q1; q += 32) {
+    const uint4 va = a4[q];
+    const int32_t wb = 2 * q - d;  // B-relative index of A's word 2q
+    unsigned long long b_lo, b_hi;
+    if ((d & 1) == 0) {
+      const uint4 vb = b4[wb >> 1];
+      b_lo = lo64(vb);
+      b_hi = hi64(vb);
+    } else {
+      const int32_t last = (int32_t)((blen + 1) >> 1) - 1;
+      b_lo = hi64(b4[max((wb - 1) >> 1, 0)]);
+      b_hi = lo64(b4[min((wb + 1) >> 1, last)]);
+    }
+    const uint32_t w0 = a0 + 2 * (uint32_t)q;
+    unsigned long long x0 = lo64(va) & b_lo, x1 = hi64(va) & b_hi;
+    if (w0 < lo) x0 = 0ull;
+    if (w0 == mw) x0 &= mmask;
+    if (w0 + 1 >= hi) x1 = 0ull;
+    if (w0 + 1 == mw) x1 &= mmask;
+    c += __popcll(x0) + __popcll(x1);
+  }
+  return c;
+}
+
+// Exclusive prefix sum of x over the warp's lanes (all lanes active).
+__device__ __forceinline__ uint32_t warp_exclusive_scan(uint32_t x, uint32_t lane) {
+  uint32_t inc = x;
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= (uint32_t)d) inc += t;
+  }
+  return inc - x;
+}
+
+// Writes the elements of word pair (lo, hi) -- absolute word index w0 for lo --
+// to list[pos...] in ascending order.
+__device__ __forceinline__ void emit_pair_bits(unsigned long long lo, unsigned long long hi, uint32_t w0,
+                                               uint32_t* list, uint32_t pos) {
+  while (lo) {
+    list[pos++] = 64u * w0 + (uint32_t)(__ffsll((long long)lo) - 1);
+    lo &= lo - 1ull;
+  }
+  while (hi) {
+    list[pos++] = 64u * (w0 + 1) + (uint32_t)(__ffsll((long long)hi) - 1);
+    hi &= hi - 1ull;
+  }
 }
 
 // First position in a[lo, hi) with a[pos] >= x (a sorted ascending).
@@ -108,6 +209,82 @@ __device__ __forceinline__ uint32_t lower_bound_u16(const uint16_t* a, uint32_t 
     if (a[mid] < x) lo = mid + 1; else hi = mid;
   }
   return lo;
+}
+
+// ---- uint ∩ uint: warp merge path ----
+// Per-lane count of the elements common to sorted A[0, na) and B[0, nb): the
+// merge of the two lists (ties: A first) is cut into 32 runs of equal length;
+// each lane finds where its run starts by a binary search along its cross
+// diagonal (Green, McColl, Bader, "GPU merge path", ICS 2012), then merges the
+// run sequentially and counts A[i] == B[j] when it takes A[i], so each match
+// is counted by exactly one lane.  The GPU form of the reference's block merge
+// set_intersect_standard (intersection.hpp:696-771), which it uses for pairs
+// whose sizes differ by at most 32x (:1325-1336).
+__device__ __forceinline__ uint32_t merge_path_lane(const uint32_t* A, uint32_t na, const uint32_t* B, uint32_t nb,
+                                                    uint32_t lane) {
+  const uint32_t total = na + nb, per = (total + 31) >> 5;
+  uint32_t d = min(total, lane * per);
+  const uint32_t dend = min(total, d + per);
+  uint32_t lo = d > nb ? d - nb : 0u, hi = min(d, na);
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (A[mid] <= B[d - mid - 1]) lo = mid + 1;
+    else hi = mid;
+  }
+  uint32_t i = lo, j = d - lo, c = 0;
+  for (; d < dend; d++) {
+    if (j >= nb || (i < na && A[i] <= B[j])) {
+      c += (j < nb && A[i] == B[j]);
+      i++;
+    } else {
+      j++;
+    }
+  }
+  return c;
+}
+
+// ---- pshort: partition headers staged in shared memory ----
+// A warp probing many elements into one pshort row first copies that row's
+// partition headers (the 16-bit high half and the header's position, at most
+// kPshortHdrCap partitions) into a per-warp table; each probe is then a
+// binary search of the highs in the table and of the low shorts inside the
+// matched partition, instead of a walk over the row's headers per element
+// (the partition match of intersection.hpp:829-878).
+constexpr uint32_t kPshortHdrCap = 64;
+struct PshortHdr {
+  uint32_t hi[kPshortHdrCap];
+  uint32_t pos[kPshortHdrCap];
+};
+// Lane 0 walks the headers of V (V.aux partitions, <= kPshortHdrCap) into t.
+__device__ __forceinline__ void pshort_stage(const RowView& V, PshortHdr* t, uint32_t lane) {
+  if (lane == 0) {
+    const uint16_t* s = static_cast<const uint16_t*>(V.p);
+    uint32_t i = 0;
+    for (uint32_t k = 0; k < V.aux; k++) {
+      t->hi[k] = s[i];
+      t->pos[k] = i;
+      i += (uint32_t)s[i + 1] + 3;
+    }
+  }
+  __syncwarp();
+}
+// Index in t of the partition with high half h, or -1.
+__device__ __forceinline__ int pshort_find(const PshortHdr* t, uint32_t parts, uint32_t h) {
+  uint32_t lo = 0, hi = parts;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (t->hi[mid] < h) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < parts && t->hi[lo] == h) ? (int)lo : -1;
+}
+__device__ __forceinline__ bool pshort_contains_staged(const RowView& V, const PshortHdr* t, uint32_t x) {
+  const int k = pshort_find(t, V.aux, x >> 16);
+  if (k < 0) return false;
+  const uint16_t* s = static_cast<const uint16_t*>(V.p) + t->pos[k];
+  const uint32_t cnt = (uint32_t)s[1] + 1, lo = x & 0xffffu;
+  const uint32_t pos = lower_bound_u16(s + 2, 0, cnt, lo);
+  return pos < cnt && s[2 + pos] == lo;
 }
 
 // Membership of one element in a row, by the row's layout.
@@ -156,15 +333,25 @@ __device__ __forceinline__ void warp_for_each(const RowView& V, uint32_t lim, ui
       f(x);
     }
   } else if (V.type == TY_BITSET) {
-    const unsigned long long* w = static_cast<const unsigned long long*>(V.p);
-    for (uint32_t k = lane; k < V.len; k += 32) {
-      uint64_t base = 64ull * (V.aux + k);
+    const int32_t np = (int32_t)((V.len + 1) >> 1);  // 16-byte word pairs
+    for (int32_t q = (int32_t)lane; q < np; q += 32) {
+      const uint64_t base = 64ull * (V.aux + 2 * (uint64_t)q);
       if (base >= lim) break;
-      unsigned long long x = w[k];
-      if (base + 64 > lim) x &= (1ull << (lim - base)) - 1ull;
+      const uint4 v = ld_pair(V.p, q, np);
+      unsigned long long x = lo64(v), y = hi64(v);
+      if (base + 64 > lim) {
+        x &= (1ull << (lim - base)) - 1ull;
+        y = 0ull;
+      } else if (base + 128 > lim) {
+        y &= (1ull << (lim - base - 64)) - 1ull;
+      }
       while (x) {
         f((uint32_t)(base + (uint32_t)(__ffsll((long long)x) - 1)));
         x &= x - 1ull;
+      }
+      while (y) {
+        f((uint32_t)(base + 64 + (uint32_t)(__ffsll((long long)y) - 1)));
+        y &= y - 1ull;
       }
     }
   } else {
@@ -217,23 +404,58 @@ __device__ inline uint64_t pshort_pair_drop(const RowView& A, const RowView& B, 
 
 // |A ∩ B| as the reference's set_intersect reports it, the pshort ∩ pshort
 // u16 quirk included, computed by one warp; every lane returns the result.
-// Two bitsets are ANDed word by word over their common word range; otherwise
-// the smaller row is streamed and each element probed into the larger one.
-__device__ inline uint32_t warp_intersect_size(RowView A, RowView B, uint32_t lane) {
-  if (!A.card || !B.card) return 0;
+//  * two bitsets: 128-bit AND + popcount over their common word range;
+//  * two uint rows of sizes within 32x of each other: warp merge path;
+//  * otherwise the smaller row is streamed and each element probed into the
+//    larger one (a binary search for uint, a bit test for a bitset); a pshort
+//    larger row with 4..kPshortHdrCap partitions is probed through its headers
+//    staged in `hdr` (per-warp shared memory, may be null), and a streamed
+//    pshort row meets it partition by partition: the high halves are matched
+//    once per partition, then the lanes search the low shorts.
+// Per-lane part of |A ∩ B| for A no larger than B (not both bitsets).
+__device__ __forceinline__ uint32_t warp_intersect_small_large(const RowView& A, const RowView& B, uint32_t lane,
+                                                               PshortHdr* hdr) {
   uint32_t c = 0;
-  if (A.type == TY_BITSET && B.type == TY_BITSET) {
-    const unsigned long long* a = static_cast<const unsigned long long*>(A.p);
-    const unsigned long long* b = static_cast<const unsigned long long*>(B.p);
-    const uint32_t lo = max(A.aux, B.aux), hi = min(A.aux + A.len, B.aux + B.len);
-    for (uint32_t w = lo + lane; w < hi; w += 32) c += __popcll(a[w - A.aux] & b[w - B.aux]);
-  } else {
-    if (A.card > B.card) {
-      const RowView T = A;
-      A = B;
-      B = T;
+  if (A.type == TY_UINT && B.type == TY_UINT && B.card <= 32u * A.card) {
+    c = merge_path_lane(static_cast<const uint32_t*>(A.p), A.card, static_cast<const uint32_t*>(B.p), B.card, lane);
+  } else if (B.type == TY_PSHORT && hdr && B.aux >= 4 && B.aux <= kPshortHdrCap) {
+    pshort_stage(B, hdr, lane);
+    if (A.type == TY_PSHORT) {
+      const uint16_t* sa = static_cast<const uint16_t*>(A.p);
+      const uint16_t* sb = static_cast<const uint16_t*>(B.p);
+      for (uint32_t i = 0; i < A.len;) {
+        const uint32_t h = sa[i], cnt = (uint32_t)sa[i + 1] + 1;
+        const int k = pshort_find(hdr, B.aux, h);
+        if (k >= 0) {
+          const uint16_t* pb = sb + hdr->pos[k];
+          const uint32_t cb = (uint32_t)pb[1] + 1;
+          for (uint32_t t = lane; t < cnt; t += 32) {
+            const uint32_t lo = sa[i + 2 + t];
+            const uint32_t pos = lower_bound_u16(pb + 2, 0, cb, lo);
+            c += (pos < cb && pb[2 + pos] == lo);
+          }
+        }
+        i += cnt + 2;
+      }
+    } else {
+      warp_for_each(A, 0xffffffffu, lane, [&](uint32_t y) { c += pshort_contains_staged(B, hdr, y); });
     }
+    __syncwarp();  // the table is reused by the warp's next pair
+  } else {
     warp_for_each(A, 0xffffffffu, lane, [&](uint32_t y) { c += row_contains(B, y); });
+  }
+  return c;
+}
+
+__device__ __forceinline__ uint32_t warp_intersect_size(const RowView& A, const RowView& B, uint32_t lane,
+                                                        PshortHdr* hdr = nullptr) {
+  if (!A.card || !B.card) return 0;
+  uint32_t c;
+  if (A.type == TY_BITSET && B.type == TY_BITSET) {
+    const uint32_t lo = max(A.aux, B.aux), hi = min(A.aux + A.len, B.aux + B.len);
+    c = lo < hi ? bitset_and_lane(A.p, A.aux, B.p, B.aux, B.len, lo, hi, 0xffffffffu, 0ull, lane) : 0u;
+  } else {
+    c = A.card > B.card ? warp_intersect_small_large(B, A, lane, hdr) : warp_intersect_small_large(A, B, lane, hdr);
   }
   c = warp_sum_u32(c);
   return c - (uint32_t)pshort_pair_drop(A, B, ~0ull);
@@ -268,30 +490,29 @@ __device__ inline void cta_decode(const RowView& A, uint32_t* list, uint32_t* sc
     return;
   }
   if (A.type == TY_BITSET) {
-    // Thread t owns words [t*W/T, (t+1)*W/T); exclusive scan of their popcounts
-    // gives each thread its output position.
-    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
-    const uint32_t W = A.len;
-    const uint32_t w0 = (uint32_t)(((uint64_t)W * tid) / kThreads);
-    const uint32_t w1 = (uint32_t)(((uint64_t)W * (tid + 1)) / kThreads);
-    uint32_t c = 0;
-    for (uint32_t k = w0; k < w1; k++) c += __popcll(w[k]);
-    scan[tid] = c;
-    __syncthreads();
-    // Hillis-Steele inclusive scan over kThreads values.
-    for (uint32_t d = 1; d < kThreads; d <<= 1) {
-      const uint32_t v = tid >= d ? scan[tid - d] : 0u;
+    // Coalesced 16-byte loads, kThreads word pairs per round; a round whose
+    // pairs are all zero is skipped after one barrier, otherwise a CTA-wide
+    // scan of the per-thread popcounts gives each thread its output position.
+    const uint32_t lane = tid & 31, warp = tid >> 5, nw = kThreads / 32;
+    const int32_t np = (int32_t)((A.len + 1) >> 1);
+    uint32_t base_pos = 0;
+    for (int32_t base = 0; base < np; base += (int32_t)kThreads) {
+      const int32_t q = base + (int32_t)tid;
+      const uint4 v = ld_pair(A.p, q, np);
+      const unsigned long long x0 = lo64(v), x1 = hi64(v);
+      const uint32_t c = __popcll(x0) + __popcll(x1);
+      if (!__syncthreads_or(c)) continue;
+      const uint32_t ex = warp_exclusive_scan(c, lane);
+      if (lane == 31) scan[warp] = ex + c;
       __syncthreads();
-      scan[tid] += v;
-      __syncthreads();
-    }
-    uint32_t pos = scan[tid] - c;
-    for (uint32_t k = w0; k < w1; k++) {
-      unsigned long long x = w[k];
-      while (x) {
-        list[pos++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
-        x &= x - 1ull;
+      uint32_t woff = 0, total = 0;
+      for (uint32_t w = 0; w < nw; w++) {
+        const uint32_t t = scan[w];
+        woff += w < warp ? t : 0u;
+        total += t;
       }
+      if (c) emit_pair_bits(x0, x1, A.aux + 2u * (uint32_t)q, list, base_pos + woff + ex);
+      base_pos += total;
     }
     return;
   }
@@ -313,23 +534,18 @@ __device__ __forceinline__ void warp_decode(const RowView& A, uint32_t* list, ui
     const uint32_t* a = static_cast<const uint32_t*>(A.p);
     for (uint32_t k = lane; k < A.card; k += 32) list[k] = a[k];
   } else if (A.type == TY_BITSET) {
-    const unsigned long long* w = static_cast<const unsigned long long*>(A.p);
+    // 16-byte loads (32 word pairs = 512 bytes per warp round); rounds whose
+    // words are all zero cost one vote.
+    const int32_t np = (int32_t)((A.len + 1) >> 1);
     uint32_t pos = 0;
-    for (uint32_t base = 0; base < A.len; base += 32) {
-      const uint32_t k = base + lane;
-      unsigned long long x = k < A.len ? w[k] : 0ull;
-      const uint32_t c = __popcll(x);
-      uint32_t inc = c;
-      for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t t = __shfl_up_sync(FULL, inc, d);
-        if (lane >= (uint32_t)d) inc += t;
-      }
-      uint32_t p = pos + inc - c;
-      while (x) {
-        list[p++] = 64u * (A.aux + k) + (uint32_t)(__ffsll((long long)x) - 1);
-        x &= x - 1ull;
-      }
-      pos += __shfl_sync(FULL, inc, 31);
+    for (int32_t base = 0; base < np; base += 32) {
+      const int32_t q = base + (int32_t)lane;
+      const uint4 v = ld_pair(A.p, q, np);
+      const uint32_t c = __popcll(lo64(v)) + __popcll(hi64(v));
+      if (!__any_sync(FULL, c != 0)) continue;
+      const uint32_t ex = warp_exclusive_scan(c, lane);
+      if (c) emit_pair_bits(lo64(v), hi64(v), A.aux + 2u * (uint32_t)q, list, pos + ex);
+      pos += __shfl_sync(FULL, ex + c, 31);
     }
   } else {
     const uint16_t* s = static_cast<const uint16_t*>(A.p);

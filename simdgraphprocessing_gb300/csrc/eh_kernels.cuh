@@ -62,6 +62,8 @@ cudaError_t launch_plan(uint64_t n, const RowDesc* desc, uint32_t min_card, uint
                         uint32_t* order, uint32_t* cursor, cudaStream_t st);
 cudaError_t exclusive_scan_u32(const uint32_t* in, uint64_t n, uint32_t* out, uint32_t* tmp,
                                cudaStream_t st);
+cudaError_t launch_gather_desc(const RowDesc* desc, const uint32_t* rows, uint32_t nrows, RowDesc* out,
+                               cudaStream_t st);
 cudaError_t launch_decode_rows(const RowDesc* desc, const uint4* arena, const uint32_t* rows,
                                const unsigned long long* dst_off, uint32_t nrows, uint32_t* dst,
                                cudaStream_t st);
@@ -85,6 +87,7 @@ struct PivotArgs {
   uint32_t num_graphs;
   const unsigned long long* core;  // dense core bitmap of rows j < core_k (see core_row_offset), or null
   uint32_t core_k;
+  uint32_t core_hot_words;  // light-pivot core probes of words below this keep their L2 lines (0: no hints)
 };
 constexpr uint32_t kCtaThreads = 256;
 constexpr uint32_t kLightMax = 96;     // largest light_max: warp-wide pivots fit a slice of this size
@@ -103,17 +106,26 @@ cudaError_t launch_lollipops(const PivotArgs& a, const uint2* units, uint32_t n_
 int pivot_grid(int device);  // persistent grid: SMs x resident CTAs of the pivot kernel
 
 // Dense core: for every row j < core_k, the bits of row(j) ∩ [0, j) packed in
-// ceil(j/64) words starting at word core_row_offset(j) (a lower-triangular
-// bitmap of the highest-degree rows, which degree ordering puts first).
+// ceil(j/64) words, padded with a zero word to an even count, starting at word
+// core_row_offset(j) (a lower-triangular bitmap of the highest-degree rows,
+// which degree ordering puts first).  Every row starts on a 16-byte boundary,
+// so it can be read as 128-bit word pairs.
 constexpr uint32_t kCoreMaxK = 131072;     // 1.07 GB of bits, the tuner's largest core
 constexpr uint32_t kCoreDefaultK = 65536;  // 268 MB: the core of a matrix the tuner has not seen
 // Heavy pivots keep their elements below min(core_k, kCoreAndMax) as bits in
 // shared memory, to AND with core rows in that range.
 constexpr uint32_t kCoreAndMax = 65536;
+__host__ __device__ inline uint32_t core_row_words(uint32_t j) {  // ceil(j / 64), rounded up to even
+  const uint32_t w = (j + 63) >> 6;
+  return w + (w & 1);
+}
 __host__ __device__ inline uint64_t core_row_offset(uint32_t j) {
+  // sum over x < j of core_row_words(x): with j - 1 = 64 a + b, the rows
+  // x = 1 .. 64 a come in a blocks of 64 rows of ceil(x / 64) = 1 .. a words
+  // (each rounded up to even), then b rows of a + 1 words (rounded up).
   if (j == 0) return 0;
   const uint64_t a = (uint64_t)(j - 1) >> 6, b = (uint64_t)(j - 1) & 63;
-  return 32 * a * (a + 1) + b * (a + 1);  // sum over x < j of ceil(x / 64)
+  return 32 * a * (a + 1) + 64 * ((a + 1) >> 1) + b * ((a + 1) + ((a + 1) & 1));
 }
 cudaError_t launch_core_build(const RowDesc* desc, const uint4* arena, uint32_t core_k, unsigned long long* core,
                               cudaStream_t st);

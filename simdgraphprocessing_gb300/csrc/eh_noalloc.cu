@@ -22,7 +22,15 @@
 // Host code cannot use the array's name as a device address (in host code it
 // is a host-side stand-in).  The first call on each device, with that device
 // current, looks its address up once with cudaGetSymbolAddress; that first
-// call should come before any stream capture.
+// call should come before any stream capture.  The address is kept for the
+// life of the process: a device reset (cudaDeviceReset) after the first call
+// is not supported, since the module and its array are loaded again then.
+//
+// The shared-memory tier runs as one launch sized for its largest pivot
+// (eh_count_cliques_async splits it into size bands with their own occupancy),
+// so on skewed graphs this entry point can be slower.  It records no use on
+// the matrix: eh_matrix_free does not wait for its launches, so the caller
+// synchronizes their stream before freeing the matrix.
 #include <algorithm>
 #include <cstdint>
 #include <mutex>

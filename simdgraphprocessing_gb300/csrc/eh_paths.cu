@@ -76,11 +76,12 @@ __device__ __forceinline__ uint32_t merge_count(const uint32_t* a, uint32_t na, 
 // kSymTiny entries (most rows of a sparse graph) or one side is empty; rows
 // above that go to the whole warp, and rows too long for a warp to the list
 // of k_symbiosity_heavy.
-__global__ void __launch_bounds__(256, 6) k_symbiosity(uint32_t n, const RowDesc* __restrict__ dr,
+__global__ void __launch_bounds__(256, 5) k_symbiosity(uint32_t n, const RowDesc* __restrict__ dr,
                                                     const uint4* __restrict__ ar, const RowDesc* __restrict__ dc,
                                                     const uint4* __restrict__ ac, double threshold,
                                                     unsigned long long* out, uint32_t* heavy, uint32_t* n_heavy,
                                                     uint32_t* cursor) {
+  __shared__ PshortHdr s_hdr[8];
   const uint32_t lane = threadIdx.x & 31;
   unsigned long long acc = 0;
   for (;;) {
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(256, 6) k_symbiosity(uint32_t n, const RowDesc
       const uint32_t r2 = base + (__ffs(wm) - 1);
       const RowView A = load_view(dr, ar, r2);
       const RowView B = load_view(dc, ac, r2);
-      const uint32_t both = warp_intersect_size(A, B, lane);
+      const uint32_t both = warp_intersect_size(A, B, lane, &s_hdr[threadIdx.x >> 5]);  // header table: pshort rows
       if (lane == 0) acc += sym_above(both, A, B, threshold);
     }
   }
@@ -383,6 +384,8 @@ extern "C" eh_status eh_symbiosity_async(eh_matrix_t rh, eh_matrix_t ch, double 
   }
   const cudaError_t ef = cudaFreeAsync(scratch, st);
   if (e == cudaSuccess) e = ef;
+  note_use(r, st);
+  note_use(c, st);
   return e == cudaSuccess ? EH_OK : cuda_err(e, "symbiosity kernels");
 }
 

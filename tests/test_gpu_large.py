@@ -58,10 +58,11 @@ def test_batch_graphs_equal_reference_binary(eh):
     G = 512
     csrs = [eh.graph(kind, s, **kw).csr()[:2] for kind, s, kw in W.batch_specs()[:G]]
     gr, off, nbr = eh.concat_graphs(csrs)
-    b = eh.Batch(gr, off, nbr, layout="hybrid")
+    s = torch.cuda.Stream()
+    b = eh.Batch(gr, off, nbr, layout="hybrid", stream=s)
     tri = torch.zeros(G, dtype=torch.int64, device="cuda")
     clq = torch.zeros(G, dtype=torch.int64, device="cuda")
-    b.run(tri.data_ptr(), clq.data_ptr(), use_graph=True)
-    torch.cuda.synchronize()
+    b.run(tri.data_ptr(), clq.data_ptr(), use_graph=True, stream=s)  # captured and replayed
+    s.synchronize()
     assert tri.cpu().tolist() == fx["triangles"][:G]
     assert clq.cpu().tolist() == fx["cliques4"][:G]

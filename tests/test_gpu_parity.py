@@ -292,3 +292,34 @@ def test_device_waits_are_bounded(eh):
     assert flag.value == 1
     off, nbr = csr(eh, "rmat10")
     assert eh.Matrix.build(off, nbr, selection="lower").count_triangles() > 0
+
+
+def test_bitset_pairs_at_every_word_alignment(eh):
+    """Bitset ∩ bitset over 16-byte word pairs: rows whose first words differ by
+    even and odd amounts, odd and even word counts, single words and long
+    sparse rows, against numpy (integer counts, tolerance 0)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    n = 1 << 17
+    rows = []
+    for r in range(96):
+        first = int(rng.integers(0, 40)) * 64 + int(rng.integers(0, 64))
+        span = int(rng.choice([1, 63, 64, 65, 130, 700, 5000, 60000]))
+        k = max(1, min(span, int(rng.integers(1, 300))))
+        vals = np.unique(np.concatenate([[first], first + rng.integers(0, span, k)]))
+        rows.append(vals[vals < n].astype(np.uint32))
+    rows += [np.zeros(0, np.uint32)] * (n - len(rows))
+    off = np.zeros(n + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in rows])
+    nbr = np.concatenate(rows).astype(np.uint32)
+    m = eh.Matrix.build(off, nbr, selection="all", layout="bs")
+    a = np.repeat(np.arange(96, dtype=np.uint32), 96)
+    b = np.tile(np.arange(96, dtype=np.uint32), 96)
+    da = torch.from_numpy(a.astype(np.int32)).cuda()
+    db = torch.from_numpy(b.astype(np.int32)).cuda()
+    dc = torch.zeros(len(a), dtype=torch.int32, device="cuda")
+    m.intersect_rows(da.data_ptr(), db.data_ptr(), len(a), dc.data_ptr())
+    torch.cuda.synchronize()
+    got = dc.cpu().numpy()
+    want = np.array([len(np.intersect1d(rows[x], rows[y])) for x, y in zip(a, b)])
+    assert np.array_equal(got, want)

@@ -7,6 +7,7 @@ the call allocates; its counts must equal eh_count_cliques's, exactly
 
 Kept in its own file, collected last."""
 import ctypes as C
+from math import comb
 
 import numpy as np
 import pytest
@@ -31,18 +32,26 @@ def complete_graphs(sizes, seed=9):
     return off, nbr
 
 
+SIZES = [1900, 600, 200, 30]
+
+
 def graphs(eh):
-    g = eh.HostGraph.from_csr(*complete_graphs([1900, 600, 200, 30])).reorder_by_degree()
+    g = eh.HostGraph.from_csr(*complete_graphs(SIZES)).reorder_by_degree()
     yield "complete", g.csr()[:2]  # pivots above ~1,850 entries (too big for shared memory) use the fixed scratch
     yield "rmat", eh.graph("rmat", 12, scale=12, edges=40000).csr()[:2]
+
+
+def _entry(L):
+    f = L.eh_count_cliques_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    return f
 
 
 def test_noalloc_counts_equal_the_allocating_entry_point(eh):
     torch = pytest.importorskip("torch")
     L = eh.load()
-    f = L.eh_count_cliques_noalloc
-    f.restype = C.c_int
-    f.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    f = _entry(L)
     for name, (off, nbr) in graphs(eh):
         m = eh.Matrix.build(off, nbr, selection="lower", layout="hybrid")
         fresh = torch.zeros(1, dtype=torch.int64, device="cuda")
@@ -57,3 +66,33 @@ def test_noalloc_counts_equal_the_allocating_entry_point(eh):
                 assert st == 0, L.eh_last_error()
             torch.cuda.synchronize()
             assert out.tolist() == [want, want], (name, k)
+            if name == "complete":  # disjoint complete graphs: sum of C(s, k)
+                assert want == sum(comb(s, k) for s in SIZES), k
+
+
+def test_noalloc_rejects_a_pivot_beyond_the_fixed_scratch(eh):
+    """A star whose hub has the highest id has one pivot of 16,400 entries: its
+    4-clique working set (about 16.9 MB) is larger than the 16 MiB array, so the
+    call refuses with EH_ERR_UNSUPPORTED and names the limit; the allocating
+    entry point counts it (0 cliques)."""
+    torch = pytest.importorskip("torch")
+    L = eh.load()
+    f = _entry(L)
+    leaves = 16400
+    hub = leaves
+    off = np.concatenate([np.arange(leaves + 1, dtype=np.uint64), [2 * leaves]]).astype(np.uint64)
+    nbr = np.concatenate([np.full(leaves, hub, np.uint32), np.arange(leaves, dtype=np.uint32)])
+    m = eh.Matrix.build(off, nbr, selection="lower", layout="hybrid")
+    assert m.count_cliques(4) == 0  # builds the plan; the allocating path has no such limit
+    out = torch.full((1,), 7, dtype=torch.int64, device="cuda")
+    assert f(m.h, 4, C.c_void_p(out.data_ptr()), None) == 4  # EH_ERR_UNSUPPORTED
+    assert b"fixed scratch" in L.eh_last_error()
+    torch.cuda.synchronize()
+    assert out.item() == 0  # the count was cleared before the size check
+    # the array is still usable: a graph that fits counts right after the refusal
+    g = eh.HostGraph.from_csr(*complete_graphs([40])).csr()[:2]
+    m2 = eh.Matrix.build(*g, selection="lower", layout="hybrid")
+    m2.count_cliques(4)
+    assert f(m2.h, 4, C.c_void_p(out.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert out.item() == comb(40, 4)
