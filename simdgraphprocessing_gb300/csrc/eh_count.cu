@@ -125,37 +125,6 @@ __device__ __forceinline__ uint32_t pair_count_stream(const uint32_t* L, uint32_
   return c;
 }
 
-// |{t < e : L[t] in row(j)}| for j in the dense core, by one lane.  Core row
-// j holds row(j) ∩ [0, j) as bits: AND it with the pivot's staged bits when j
-// is within them and that takes no more steps (ceil(wj / 2) 128-bit word
-// pairs) than probing it at the e pivot elements below j, else probe.  (At
-// R-MAT scale 22, 29.6 M pairs AND and 5.6 M probe; streaming row(j) into the
-// pivot instead would be cheaper for none of them.)
-__device__ __forceinline__ uint32_t core_pair_lane(const PivotArgs& a, const uint32_t* L, uint32_t e, uint32_t j,
-                                                   uint32_t and_k, const unsigned long long* abits) {
-  const unsigned long long* row = a.core + core_row_offset(j);
-  const uint32_t np = (((j + 63) >> 6) + 1) >> 1;
-  uint32_t cnt = 0;
-  if (j <= and_k && np <= e) {
-    // The core row starts 16-byte aligned and ends in a zero pad word; the
-    // staged bits are 16-byte aligned.
-    const uint4* r4 = reinterpret_cast<const uint4*>(row);
-    const uint4* b4 = reinterpret_cast<const uint4*>(abits);
-#pragma unroll 1
-    for (uint32_t q = 0; q < np; q++) {
-      const uint4 x = b4[q], y = __ldg(r4 + q);
-      cnt += __popcll(lo64(x) & lo64(y)) + __popcll(hi64(x) & hi64(y));
-    }
-    return cnt;
-  }
-#pragma unroll 1
-  for (uint32_t t = 0; t < e; t++) {
-    const uint32_t x = L[t];
-    cnt += (uint32_t)((__ldg(row + (x >> 6)) >> (x & 63)) & 1ull);
-  }
-  return cnt;
-}
-
 // Heavy pivots: 6 resident CTAs per SM, 40 registers per thread (the per-pair
 // choice keeps many values live, and at 32 registers it spilled).
 template <bool LOLLI>
@@ -220,34 +189,52 @@ __global__ void __launch_bounds__(kCtaThreads, 6) k_pivots_heavy(PivotArgs a, co
     const uint32_t e0 = 1 + uu.y * a.unit_span;
     const uint32_t e1 = min(c, e0 + a.unit_span);
     unsigned long long uacc = 0;
-    // Pairs (i, j = L[e]) with j in the dense core run one per lane: the lane
-    // does the pair's whole AND or probe loop, so the per-pair work (core row
-    // offset, choice, reduction) is paid once per 32 pairs instead of once per
-    // pair.  Pairs outside the core are collected by ballot and intersected by
-    // the whole warp, each with its own layout pair.
-    for (uint32_t base = e0 + 32 * warp; base < e1; base += kCtaThreads) {
-      const uint32_t e = base + lane;
-      uint32_t j = 0;
-      bool coop = false;
-      if (e < e1) {
-        j = L[e];
-        if (use_core && j < a.core_k) {
-          const uint32_t cnt = core_pair_lane(a, L, e, j, and_k, s.abits);
-          uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
+    for (uint32_t e = e0 + warp; e < e1; e += NWARPS) {
+      const uint32_t j = L[e];
+      uint32_t cnt;
+      if (use_core && j < a.core_k) {
+        // Core row j holds row(j) ∩ [0, j).  Cheapest of: AND it with the pivot's
+        // bits (j within the staged bits; wj words), probe it at the e pivot
+        // elements below j (e words), or stream row(j) itself and look each
+        // element up in the pivot (|row(j)| lookups; rows past the highest-degree
+        // ones are short while e grows with the pivot).
+        const unsigned long long* row = a.core + core_row_offset(j);
+        const uint32_t wj = (j + 63) >> 6;
+        cnt = 0;
+        if (j <= and_k && wj <= e) {
+          // 128-bit word pairs: the core row starts 16-byte aligned and ends in
+          // a zero pad word, and the staged bits are 16-byte aligned.
+          const uint4* r4 = reinterpret_cast<const uint4*>(row);
+          const uint4* b4 = reinterpret_cast<const uint4*>(s.abits);
+#pragma unroll 2
+          for (uint32_t q = lane; q < ((wj + 1) >> 1); q += 32) {
+            const uint4 x = b4[q], y = __ldg(r4 + q);
+            cnt += __popcll(lo64(x) & lo64(y)) + __popcll(hi64(x) & hi64(y));
+          }
         } else {
-          coop = true;
+          bool stream = false;
+          RowView B;
+          if (e > kStreamMinE) {
+            B = load_view(a.desc, a.arena, j);
+            stream = (uint64_t)B.card * (A.type == TY_BITSET ? 1u : ilog2p1(e)) < e;
+          }
+          if (stream) {
+            cnt = pair_count_stream(L, e, A, B, j, lane);
+          } else {
+            for (uint32_t t = lane; t < e; t += 32) {
+              const uint32_t x = L[t];
+              cnt += (uint32_t)((__ldg(row + (x >> 6)) >> (x & 63)) & 1ull);
+            }
+          }
         }
+        cnt = warp_sum_u32(cnt);
+      } else {
+        const RowView B = load_view(a.desc, a.arena, j);
+        cnt = pair_count_warp(L, e, A, B, j, lane);
       }
-      for (uint32_t pend = __ballot_sync(FULL, coop); pend; pend &= pend - 1) {
-        const uint32_t src = __ffs(pend) - 1;
-        const uint32_t jj = __shfl_sync(FULL, j, src);
-        const RowView B = load_view(a.desc, a.arena, jj);
-        const uint32_t cnt = pair_count_warp(L, base + src, A, B, jj, lane);
-        if (lane == 0) uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
-      }
+      if (lane == 0) uacc += LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
     }
     if (a.graph_rows) {  // batch: this unit's count goes to its graph
-      uacc = warp_sum_u64(uacc);
       if (lane == 0 && uacc) atomicAdd(&a.out[graph_of(a.graph_rows, a.num_graphs, i)], uacc);
     } else {
       acc += uacc;
