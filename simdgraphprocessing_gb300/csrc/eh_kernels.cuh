@@ -106,26 +106,17 @@ cudaError_t launch_lollipops(const PivotArgs& a, const uint2* units, uint32_t n_
 int pivot_grid(int device);  // persistent grid: SMs x resident CTAs of the pivot kernel
 
 // Dense core: for every row j < core_k, the bits of row(j) ∩ [0, j) packed in
-// ceil(j/64) words, padded with a zero word to an even count, starting at word
-// core_row_offset(j) (a lower-triangular bitmap of the highest-degree rows,
-// which degree ordering puts first).  Every row starts on a 16-byte boundary,
-// so it can be read as 128-bit word pairs.
+// ceil(j/64) words starting at word core_row_offset(j) (a lower-triangular
+// bitmap of the highest-degree rows, which degree ordering puts first).
 constexpr uint32_t kCoreMaxK = 131072;     // 1.07 GB of bits, the tuner's largest core
 constexpr uint32_t kCoreDefaultK = 65536;  // 268 MB: the core of a matrix the tuner has not seen
 // Heavy pivots keep their elements below min(core_k, kCoreAndMax) as bits in
 // shared memory, to AND with core rows in that range.
 constexpr uint32_t kCoreAndMax = 65536;
-__host__ __device__ inline uint32_t core_row_words(uint32_t j) {  // ceil(j / 64), rounded up to even
-  const uint32_t w = (j + 63) >> 6;
-  return w + (w & 1);
-}
 __host__ __device__ inline uint64_t core_row_offset(uint32_t j) {
-  // sum over x < j of core_row_words(x): with j - 1 = 64 a + b, the rows
-  // x = 1 .. 64 a come in a blocks of 64 rows of ceil(x / 64) = 1 .. a words
-  // (each rounded up to even), then b rows of a + 1 words (rounded up).
   if (j == 0) return 0;
   const uint64_t a = (uint64_t)(j - 1) >> 6, b = (uint64_t)(j - 1) & 63;
-  return 32 * a * (a + 1) + 64 * ((a + 1) >> 1) + b * ((a + 1) + ((a + 1) & 1));
+  return 32 * a * (a + 1) + b * (a + 1);  // sum over x < j of ceil(x / 64)
 }
 cudaError_t launch_core_build(const RowDesc* desc, const uint4* arena, uint32_t core_k, unsigned long long* core,
                               cudaStream_t st);
