@@ -288,6 +288,9 @@ typedef struct eh_tuning {
   uint32_t core_hot_words; /* light-pivot probes of the first words of each dense-core
                               row keep their L2 lines, the rest are evicted first
                               (0 = no cache hints)                                  */
+  uint32_t core_filter_words; /* words of the per-row hashed filter checked before a
+                              light-pivot probe reads a dense-core word: 0 (none),
+                              16, 32 or 64                                          */
 } eh_tuning;
 /* Times the triangle count (EH_SELECT_LOWER) or the lollipop count
  * (EH_SELECT_ALL) on this matrix for a small set of work shapes, coordinate by
@@ -296,7 +299,7 @@ typedef struct eh_tuning {
  * EH_TUNE_CACHE, if set). */
 eh_status eh_matrix_tune(eh_matrix_t m, void* stream, eh_tuning* result);
 /* Uses the given work shape (light_max, unit_span, ctas_per_sm, core_rows,
- * core_hot_words of `shape`; ms and configs_tried are ignored) for this
+ * core_hot_words, core_filter_words of `shape`; ms and configs_tried are ignored) for this
  * matrix's later counts, rebuilding its plan as needed.  Counts do not depend
  * on the shape.  EH_ERR_INVALID_ARGUMENT for a value outside the tuner's
  * ranges.  (No reference counterpart.) */

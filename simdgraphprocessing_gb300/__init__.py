@@ -35,7 +35,7 @@ class EHError(RuntimeError):
 class Tuning(C.Structure):
     _fields_ = [("light_max", C.c_uint32), ("unit_span", C.c_uint32), ("ctas_per_sm", C.c_uint32),
                 ("core_rows", C.c_uint32), ("ms", C.c_float), ("configs_tried", C.c_uint32),
-                ("core_hot_words", C.c_uint32)]
+                ("core_hot_words", C.c_uint32), ("core_filter_words", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):
@@ -442,10 +442,11 @@ class Matrix:
         check(load().eh_matrix_tune(self.h, _stream(stream), C.byref(t)))
         return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
-    def set_shape(self, light_max, unit_span, ctas_per_sm, core_rows, core_hot_words=0, stream=None):
+    def set_shape(self, light_max, unit_span, ctas_per_sm, core_rows, core_hot_words=0, core_filter_words=0,
+                  stream=None):
         """Uses this work shape for later counts (eh_matrix_set_shape)."""
         t = Tuning(light_max=light_max, unit_span=unit_span, ctas_per_sm=ctas_per_sm, core_rows=core_rows,
-                   core_hot_words=core_hot_words)
+                   core_hot_words=core_hot_words, core_filter_words=core_filter_words)
         check(load().eh_matrix_set_shape(self.h, C.byref(t), _stream(stream)))
 
     def intersect_rows(self, d_a, d_b, npairs, d_counts, stream=None):

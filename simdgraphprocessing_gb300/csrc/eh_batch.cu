@@ -44,7 +44,7 @@ struct Batch {
 namespace {
 
 struct Shape {
-  uint32_t light_max, unit_span, ctas, core, hot;
+  uint32_t light_max, unit_span, ctas, core, hot, filter;
 };
 
 std::mutex g_tune_mutex;
@@ -74,11 +74,11 @@ void load_tune_file() {
   FILE* f = fopen(path, "r");
   if (!f) return;
   char line[1024];
-  while (fgets(line, sizeof(line), f)) {  // key light_max unit_span ctas core [hot]
+  while (fgets(line, sizeof(line), f)) {  // key light_max unit_span ctas core [hot [filter]]
     char key[512];
-    unsigned lm, us, ct, co, hot = 0;
-    if (sscanf(line, "%511s %u %u %u %u %u", key, &lm, &us, &ct, &co, &hot) >= 5)
-      g_tune_cache[key] = Shape{lm, us, ct, co, hot};
+    unsigned lm, us, ct, co, hot = 0, filt = 0;
+    if (sscanf(line, "%511s %u %u %u %u %u %u", key, &lm, &us, &ct, &co, &hot, &filt) >= 5)
+      g_tune_cache[key] = Shape{lm, us, ct, co, hot, filt};
   }
   fclose(f);
 }
@@ -89,7 +89,7 @@ void store_tune(const std::string& key, const Shape& s) {
   if (!path) return;
   FILE* f = fopen(path, "a");
   if (!f) return;
-  fprintf(f, "%s %u %u %u %u %u\n", key.c_str(), s.light_max, s.unit_span, s.ctas, s.core, s.hot);
+  fprintf(f, "%s %u %u %u %u %u %u\n", key.c_str(), s.light_max, s.unit_span, s.ctas, s.core, s.hot, s.filter);
   fclose(f);
 }
 
@@ -106,6 +106,7 @@ eh_status apply_shape(Matrix* m, const Shape& s, cudaStream_t st) {
   m->unit_span = s.unit_span;
   m->core_limit = s.core;
   m->core_hot_words = s.hot;
+  m->core_filter_words = s.filter;
   m->grid = sms * (int)s.ctas;
   return ensure_plan(m, st);
 }
@@ -151,7 +152,8 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
   if (pool_alloc((void**)&out, outn * sizeof(unsigned long long), st) != cudaSuccess)
     return set_error(EH_ERR_OUT_OF_MEMORY, "tuner output allocation failed");
   auto it = g_tune_cache.find(key);
-  Shape best{m->light_max, m->unit_span, (uint32_t)max_ctas_per_sm(m->device), m->core_limit, m->core_hot_words};
+  Shape best{m->light_max, m->unit_span, (uint32_t)max_ctas_per_sm(m->device), m->core_limit, m->core_hot_words,
+             m->core_filter_words};
   float best_ms = 0;
   uint32_t tried = 0;
   if (it != g_tune_cache.end()) {
@@ -176,24 +178,34 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
       }
     };
     const Shape start = best;
-    for (uint32_t co : {0u, 16384u, 32768u, 65536u, 98304u, 131072u})
-      if (co != start.core && co <= kCoreMaxK) consider(Shape{start.light_max, start.unit_span, start.ctas, co, start.hot});
+    // Core size and filters together: a filter makes a larger core pay.
+    for (uint32_t co : {0u, 16384u, 32768u, 65536u, 98304u, 131072u, 196608u, 262144u})
+      for (uint32_t fw : {0u, 32u})
+        if ((co != start.core || fw != start.filter) && co <= kCoreMaxK && (fw == 0 || co > kFilterLo))
+          consider(Shape{start.light_max, start.unit_span, start.ctas, co, start.hot, fw});
     const Shape after_core0 = best;
     if (after_core0.core)
       for (uint32_t hot : {0u, 32u, 64u, 128u})
         if (hot != after_core0.hot)
-          consider(Shape{after_core0.light_max, after_core0.unit_span, after_core0.ctas, after_core0.core, hot});
+          consider(Shape{after_core0.light_max, after_core0.unit_span, after_core0.ctas, after_core0.core, hot,
+                         after_core0.filter});
+    const Shape after_hot = best;
+    if (after_hot.core > kFilterLo)
+      for (uint32_t fw : {0u, 16u, 32u, 64u})
+        if (fw != after_hot.filter)
+          consider(Shape{after_hot.light_max, after_hot.unit_span, after_hot.ctas, after_hot.core, after_hot.hot, fw});
     const Shape after_core = best;
     for (int c = 1; c <= cmax; c++)
       if ((uint32_t)c != after_core.ctas)
-        consider(Shape{after_core.light_max, after_core.unit_span, (uint32_t)c, after_core.core, after_core.hot});
+        consider(Shape{after_core.light_max, after_core.unit_span, (uint32_t)c, after_core.core, after_core.hot,
+                         after_core.filter});
     const Shape after_ctas = best;
     for (uint32_t lm : {32u, 64u, 96u})
       if (lm != after_ctas.light_max && lm <= kLightMax)
-        consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas, after_ctas.core, after_ctas.hot});
+        consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas, after_ctas.core, after_ctas.hot, after_ctas.filter});
     const Shape after_lm = best;
     for (uint32_t us : {32u, 128u, 256u, 512u, 1024u, 2048u})
-      if (us != after_lm.unit_span) consider(Shape{after_lm.light_max, us, after_lm.ctas, after_lm.core, after_lm.hot});
+      if (us != after_lm.unit_span) consider(Shape{after_lm.light_max, us, after_lm.ctas, after_lm.core, after_lm.hot, after_lm.filter});
     if (s == EH_OK) {
       s = apply_shape(m, best, st);
       store_tune(key, best);
@@ -209,6 +221,7 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
     res->ms = best_ms;
     res->configs_tried = tried;
     res->core_hot_words = best.hot;
+    res->core_filter_words = best.filter;
   }
   return EH_OK;
 }
@@ -228,6 +241,7 @@ void apply_cached_shape(Matrix* m) {
   m->unit_span = it->second.unit_span;
   m->core_limit = it->second.core;
   m->core_hot_words = it->second.hot;
+  m->core_filter_words = it->second.filter;
   m->grid = sms * (int)it->second.ctas;
 }
 
@@ -259,7 +273,10 @@ eh_status eh_matrix_set_shape(eh_matrix_t mh, const eh_tuning* shape, void* stre
   EH_CHECK_ARG(shape->ctas_per_sm >= 1 && (int)shape->ctas_per_sm <= eh::max_ctas_per_sm(m->device),
                "ctas_per_sm %u outside [1, %d]", shape->ctas_per_sm, eh::max_ctas_per_sm(m->device));
   EH_CHECK_ARG(shape->core_rows <= eh::kCoreMaxK, "core_rows %u above %u", shape->core_rows, eh::kCoreMaxK);
-  const eh::Shape s{shape->light_max, shape->unit_span, shape->ctas_per_sm, shape->core_rows, shape->core_hot_words};
+  const uint32_t fw = shape->core_filter_words;
+  EH_CHECK_ARG(fw == 0 || fw == 16 || fw == 32 || fw == 64, "core_filter_words %u is not 0, 16, 32 or 64", fw);
+  const eh::Shape s{shape->light_max, shape->unit_span, shape->ctas_per_sm, shape->core_rows, shape->core_hot_words,
+                    fw};
   return eh::apply_shape(m, s, reinterpret_cast<cudaStream_t>(stream));
 }
 

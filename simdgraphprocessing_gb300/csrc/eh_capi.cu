@@ -280,21 +280,41 @@ eh_status ensure_core(Matrix* m, cudaStream_t st) {
   Plan& p = m->plan;
   uint32_t want = (uint32_t)std::min<uint64_t>(m->n, m->core_limit) & ~63u;
   if (m->n < 4096) want = 0;
-  if (want == p.core_k && (want == 0 || p.core)) return EH_OK;
-  if (p.core) {  // launches on other streams may still read it
-    CU(wait_uses(m, st), "core");
+  // Row filters cover the core's rows from kFilterLo on.
+  const uint32_t want_fw = (m->core_filter_words && want > kFilterLo) ? m->core_filter_words : 0u;
+  const uint32_t want_fk = want_fw ? want : 0u;
+  if (want == p.core_k && (want == 0 || p.core) && want_fw == p.filter_words && want_fk == p.filter_k)
+    return EH_OK;
+  if (p.core || p.filter) CU(wait_uses(m, st), "core");  // launches on other streams may still read them
+  if (p.filter) {
+    CU(cudaFreeAsync(p.filter, st), "row filters");
+    m->device_bytes -= (uint64_t)(p.filter_k - kFilterLo) * p.filter_words * 8;
+    p.filter = nullptr;
+    p.filter_words = 0;
+    p.filter_k = 0;
+  }
+  if (p.core && want != p.core_k) {
     CU(cudaFreeAsync(p.core, st), "core");
     m->device_bytes -= core_row_offset(p.core_k) * 8;
     p.core = nullptr;
     p.core_k = 0;
   }
-  if (want == 0) return EH_OK;
-  const uint64_t words = core_row_offset(want);
-  CU(pool_alloc((void**)&p.core, words * 8, st), "core allocation");
-  m->device_bytes += words * 8;
-  CU(launch_core_build(m->desc, m->arena, want, p.core, st), "core build");
+  if (want && !p.core) {
+    const uint64_t words = core_row_offset(want);
+    CU(pool_alloc((void**)&p.core, words * 8, st), "core allocation");
+    m->device_bytes += words * 8;
+    CU(launch_core_build(m->desc, m->arena, want, p.core, st), "core build");
+    p.core_k = want;
+  }
+  if (want_fw) {
+    const uint64_t fwords = (uint64_t)(want_fk - kFilterLo) * want_fw;
+    CU(pool_alloc((void**)&p.filter, fwords * 8, st), "row filter allocation");
+    m->device_bytes += fwords * 8;
+    CU(launch_filter_build(m->desc, m->arena, want_fk, want_fw, p.filter, st), "row filter build");
+    p.filter_words = want_fw;
+    p.filter_k = want_fk;
+  }
   CU(cudaStreamSynchronize(st), "core build");
-  p.core_k = want;
   return EH_OK;
 }
 
@@ -395,6 +415,9 @@ PivotArgs pivot_args(Matrix* m, unsigned long long* out) {
   a.core = m->plan.core;
   a.core_k = m->plan.core_k;
   a.core_hot_words = m->core_hot_words;
+  a.filter = m->plan.filter;
+  a.filter_words = m->plan.filter_words;
+  a.filter_k = m->plan.filter_k;
   return a;
 }
 
@@ -752,7 +775,7 @@ void eh_matrix_free(eh_matrix_t mh) {
     st = nullptr;
   }
   void* bufs[] = {m->desc, m->arena, m->counters, m->plan.order, m->plan.units, m->plan.giant_lists,
-                  m->plan.giant_off, m->plan.core, m->clique_scratch};
+                  m->plan.giant_off, m->plan.core, m->plan.filter, m->clique_scratch};
   for (void* b : bufs)
     if (b) cudaFreeAsync(b, st);
   for (auto& u : m->uses) cudaEventDestroy(u.second);

@@ -268,15 +268,22 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
       uint32_t cnt = 0;
       for (uint32_t q = lane; q < pairs; q += 32) {
         const uint32_t j = list[e], x = list[t];
-        if (j < a.core_k) {  // x < j: one word of the core row j
+        // The row's filter first (if it has one): a clear bit means x is not
+        // in row(j), and neither the core word nor the row is read.
+        bool maybe = true;
+        if (j >= kFilterLo && j < a.filter_k) {
+          const uint32_t b = filter_bit(x, a.filter_words);
+          maybe = (ld_keep(a.filter + (uint64_t)(j - kFilterLo) * a.filter_words + (b >> 6)) >> (b & 63)) & 1ull;
+        }
+        if (maybe && j < a.core_k) {  // x < j: one word of the core row j
           // With core_hot_words set, words near the start of each core row
-          // (the highest-degree columns, where most probes land) keep their L2
-          // lines and the others are evicted first.
+          // (the highest-degree columns, where most probes land) keep their
+          // L2 lines and the others are evicted first.
           const unsigned long long* p = a.core + core_row_offset(j) + (x >> 6);
           const uint32_t hot = a.core_hot_words;
           const unsigned long long w = hot == 0 ? __ldg(p) : (x >> 6) < hot ? ld_keep(p) : ld_stream(p);
           cnt += (uint32_t)((w >> (x & 63)) & 1ull);
-        } else {
+        } else if (maybe) {
           const RowView B = load_view(a.desc, a.arena, j);
           cnt += row_contains(B, x);
         }
@@ -320,6 +327,26 @@ __global__ void __launch_bounds__(256) k_core_build(const RowDesc* __restrict__ 
     } else {
       warp_for_each(B, j, lane, [&](uint32_t x) { atomicOr(&row[x >> 6], 1ull << (x & 63)); });
     }
+    __syncwarp();
+  }
+}
+
+// Row filters: one warp per row j in [kFilterLo, filter_k) sets
+// filter_bit(x) for each x in row(j) ∩ [0, j).
+__global__ void __launch_bounds__(256) k_filter_build(const RowDesc* __restrict__ desc,
+                                                      const uint4* __restrict__ arena, uint32_t filter_k,
+                                                      uint32_t filter_words, unsigned long long* __restrict__ filter) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nw = gridDim.x * (blockDim.x / 32);
+  for (uint32_t j = kFilterLo + blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); j < filter_k; j += nw) {
+    unsigned long long* row = filter + (uint64_t)(j - kFilterLo) * filter_words;
+    for (uint32_t w = lane; w < filter_words; w += 32) row[w] = 0ull;
+    __syncwarp();
+    const RowView B = load_view(desc, arena, j);
+    warp_for_each(B, j, lane, [&](uint32_t x) {
+      const uint32_t b = filter_bit(x, filter_words);
+      atomicOr(&row[b >> 6], 1ull << (b & 63));
+    });
     __syncwarp();
   }
 }
@@ -442,6 +469,14 @@ cudaError_t launch_core_build(const RowDesc* desc, const uint4* arena, uint32_t 
   if (core_k == 0) return cudaSuccess;
   const uint32_t blocks = std::min<uint32_t>((core_k + 7) / 8, 152u * 16u);
   k_core_build<<<blocks, 256, 0, st>>>(desc, arena, core_k, core);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_filter_build(const RowDesc* desc, const uint4* arena, uint32_t filter_k, uint32_t filter_words,
+                                unsigned long long* filter, cudaStream_t st) {
+  if (filter_k <= kFilterLo || filter_words == 0) return cudaSuccess;
+  const uint32_t blocks = std::min<uint32_t>((filter_k - kFilterLo + 7) / 8, 152u * 16u);
+  k_filter_build<<<blocks, 256, 0, st>>>(desc, arena, filter_k, filter_words, filter);
   return cudaGetLastError();
 }
 

@@ -88,6 +88,9 @@ struct PivotArgs {
   const unsigned long long* core;  // dense core bitmap of rows j < core_k (see core_row_offset), or null
   uint32_t core_k;
   uint32_t core_hot_words;  // light-pivot core probes of words below this keep their L2 lines (0: no hints)
+  const unsigned long long* filter;  // row filters of rows [kFilterLo, filter_k), or null (see filter_bit)
+  uint32_t filter_words;             // words per row filter (16, 32 or 64)
+  uint32_t filter_k;
 };
 constexpr uint32_t kCtaThreads = 256;
 constexpr uint32_t kLightMax = 96;     // largest light_max: warp-wide pivots fit a slice of this size
@@ -108,7 +111,7 @@ int pivot_grid(int device);  // persistent grid: SMs x resident CTAs of the pivo
 // Dense core: for every row j < core_k, the bits of row(j) ∩ [0, j) packed in
 // ceil(j/64) words starting at word core_row_offset(j) (a lower-triangular
 // bitmap of the highest-degree rows, which degree ordering puts first).
-constexpr uint32_t kCoreMaxK = 131072;     // 1.07 GB of bits, the tuner's largest core
+constexpr uint32_t kCoreMaxK = 262144;     // 4.3 GB of bits, the largest core a shape may ask for
 constexpr uint32_t kCoreDefaultK = 65536;  // 268 MB: the core of a matrix the tuner has not seen
 // Heavy pivots keep their elements below min(core_k, kCoreAndMax) as bits in
 // shared memory, to AND with core rows in that range.
@@ -120,6 +123,26 @@ __host__ __device__ inline uint64_t core_row_offset(uint32_t j) {
 }
 cudaError_t launch_core_build(const RowDesc* desc, const uint4* arena, uint32_t core_k, unsigned long long* core,
                               cudaStream_t st);
+
+// Core row filters: for every core row j in [kFilterLo, filter_k = core_k), a
+// bitmap of filter_words * 64 bits with bit filter_bit(x) set for each x in
+// row(j) ∩ [0, j) (Fibonacci hashing: the top bits of x * 2^32 / phi).  A light
+// pivot's probe (j, x) reads the filter word first and the core word only when
+// the bit is set, so a probe that misses (about 91% of them at R-MAT scale 22)
+// costs one word of the small filter, loaded with the L2 keep hint, instead of
+// a DRAM sector of the core; that makes a larger core pay (at scale 22 the
+// tuner picks 262,144 rows with filters, 8.35 ms per count, against 98,304
+// rows without, 8.86 ms).  A set bit is only a hint: the core word decides, so
+// counts are exact.  Rows below kFilterLo form a core block small enough to
+// stay in L2 and have no filter.  (Filters on rows past the core, falling back
+// to the row's binary search, measured no faster.)
+constexpr uint32_t kFilterLo = 4096;
+__host__ __device__ inline uint32_t filter_bit(uint32_t x, uint32_t filter_words) {
+  const uint32_t log2_bits = filter_words == 16 ? 10u : filter_words == 32 ? 11u : 12u;
+  return (x * 2654435769u) >> (32 - log2_bits);
+}
+cudaError_t launch_filter_build(const RowDesc* desc, const uint4* arena, uint32_t filter_k, uint32_t filter_words,
+                                unsigned long long* filter, cudaStream_t st);
 cudaError_t launch_similar(uint64_t n, const RowDesc* desc, const uint4* arena, uint32_t vstar,
                            uint32_t threshold, unsigned long long* out, cudaStream_t st);
 cudaError_t launch_intersect_rows(uint64_t n, const RowDesc* desc, const uint4* arena, const uint32_t* a,

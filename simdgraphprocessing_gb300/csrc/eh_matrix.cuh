@@ -28,6 +28,8 @@ struct Plan {
   uint64_t units_cap = 0;
   unsigned long long* core = nullptr;  // dense core bitmap (rows j < core_k)
   uint32_t core_k = 0;
+  unsigned long long* filter = nullptr;  // row filters (rows [kFilterLo, filter_k))
+  uint32_t filter_words = 0, filter_k = 0;
   // rows in the plan with card > x (x < 65535)
   uint32_t above(uint32_t x) const { return starts.empty() ? 0 : starts[65535 - x]; }
   // largest card <= x present in the plan (0 if none)
@@ -69,6 +71,7 @@ struct Matrix {
   uint32_t unit_span = kDefaultUnitSpan;
   uint32_t core_limit = kCoreDefaultK;  // rows in the dense core at most (0 = no core)
   uint32_t core_hot_words = 0;          // see PivotArgs::core_hot_words
+  uint32_t core_filter_words = 0;       // words per core row filter (0: no filters)
   bool is_batch = false;            // the union matrix of an eh_batch_t
   // Where the matrix's buffers are read: one event per stream, recorded after
   // every launch that reads them (not while that stream is being captured).

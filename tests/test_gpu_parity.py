@@ -323,3 +323,37 @@ def test_bitset_pairs_at_every_word_alignment(eh):
     got = dc.cpu().numpy()
     want = np.array([len(np.intersect1d(rows[x], rows[y])) for x, y in zip(a, b)])
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("filter_words", [0, 16, 32, 64])
+def test_core_filters_keep_counts(eh, oracle, filter_words):
+    """The hashed filters in front of the dense core's rows (a work-shape
+    choice) never change a count: a set bit still reads the core word, a clear
+    bit means the element is absent.  Triangles and lollipops on a graph whose
+    core spans rows [0, 8192), so rows [4096, 8192) have filters, and a batch."""
+    torch = pytest.importorskip("torch")
+    off, nbr = eh.graph("rmat", 23, scale=14, edges=200000).csr()[:2]
+    low = eh.Matrix.build(off, nbr, "lower", "hybrid")
+    full = eh.Matrix.build(off, nbr, "all", "hybrid")
+    low.set_shape(96, 128, 4, 8192, 64, filter_words)
+    full.set_shape(96, 128, 4, 8192, 0, filter_words)
+    assert low.count_triangles() == oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.HYBRID).triangles()
+    assert full.count_lollipops() == oracle.Matrix(off, nbr, oracle.SELECT_ALL, oracle.HYBRID).lollipops()
+    csrs = [eh.graph("rmat", 40 + k, scale=12, edges=30000).csr()[:2] for k in range(3)]
+    gr, boff, bnbr = eh.concat_graphs(csrs)
+    b = eh.Batch(gr, boff, bnbr, layout="hybrid")
+    bm = eh.C.c_void_p()
+    eh.check(eh.load().eh_batch_matrix(b.h, eh.C.byref(bm)))
+    t = eh.Tuning(light_max=96, unit_span=128, ctas_per_sm=4, core_rows=8192, core_filter_words=filter_words)
+    eh.check(eh.load().eh_matrix_set_shape(bm, eh.C.byref(t), None))
+    tri = torch.zeros(len(csrs), dtype=torch.int64, device="cuda")
+    b.count(3, tri.data_ptr())
+    torch.cuda.synchronize()
+    assert tri.cpu().tolist() == [oracle.Matrix(o, n, oracle.SELECT_LOWER, oracle.HYBRID).triangles() for o, n in csrs]
+
+
+def test_set_shape_rejects_bad_filter_width(eh):
+    off, nbr = eh.graph("rmat", 22, scale=10, edges=5000).csr()[:2]
+    m = eh.Matrix.build(off, nbr, "lower", "hybrid")
+    with pytest.raises(eh.EHError):
+        m.set_shape(96, 128, 4, 0, 0, 24)
