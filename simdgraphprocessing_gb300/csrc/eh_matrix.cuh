@@ -88,8 +88,9 @@ struct Matrix {
 // a stream made to wait for the matrix's recorded uses (note_use / wait_uses).
 // The pool keeps up to kPoolKeep bytes of freed memory mapped between calls:
 // the device's default pool releases it at every synchronisation, and mapping
-// 400 MB again costs about 1 ms on GB300.
-constexpr uint64_t kPoolKeep = 4ull << 30;
+// 400 MB again costs about 1 ms on GB300.  16 GiB holds a rebuilt scale-22
+// matrix with its largest tuned core (4.3 GB) and its build scratch.
+constexpr uint64_t kPoolKeep = 16ull << 30;
 cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st);
 // A non-blocking stream of the current device for host uploads that overlap
 // the build (one per device, created on first use).
