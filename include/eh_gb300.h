@@ -298,10 +298,20 @@ typedef struct eh_tuning {
  * layout, selection, size bucket) in the process (and in the file named by
  * EH_TUNE_CACHE, if set). */
 eh_status eh_matrix_tune(eh_matrix_t m, void* stream, eh_tuning* result);
+/* As eh_matrix_tune, for matrices that are built, counted counts_per_build
+ * times and freed: each shape is ranked by its count time plus the one-shot
+ * cost of its own plan parts (heavy work units, dense core, row filters; host
+ * time, median of 3 builds) divided by counts_per_build, so a large core that
+ * saves less per count than it costs to build loses.  0 ranks by count time
+ * alone (eh_matrix_tune).  The choice is cached per counts_per_build beside
+ * eh_matrix_tune's and is not applied to other matrices by itself: pass it to
+ * eh_matrix_set_shape after each build.  result->ms is the count time.  (No
+ * reference counterpart.) */
+eh_status eh_matrix_tune_for(eh_matrix_t m, uint32_t counts_per_build, void* stream, eh_tuning* result);
 /* Uses the given work shape (light_max, unit_span, ctas_per_sm, core_rows,
  * core_hot_words, core_filter_words of `shape`; ms and configs_tried are ignored) for this
- * matrix's later counts, rebuilding its plan as needed.  Counts do not depend
- * on the shape.  EH_ERR_INVALID_ARGUMENT for a value outside the tuner's
+ * matrix's later counts, rebuilding its plan as needed; a cached tuned shape no
+ * longer applies to this matrix.  Counts do not depend on the shape.  EH_ERR_INVALID_ARGUMENT for a value outside the tuner's
  * ranges.  (No reference counterpart.) */
 eh_status eh_matrix_set_shape(eh_matrix_t m, const eh_tuning* shape, void* stream);
 

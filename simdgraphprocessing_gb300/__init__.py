@@ -130,6 +130,7 @@ def load(build_if_missing=True):
         "eh_selftest_bounded_wait": (I, [U32, C.POINTER(U32)]),
         "eh_list_triangles": (I, [P, P, U64, P, P]),
         "eh_matrix_tune": (I, [P, P, C.POINTER(Tuning)]),
+        "eh_matrix_tune_for": (I, [P, C.c_uint32, P, C.POINTER(Tuning)]),
         "eh_matrix_set_shape": (I, [P, C.POINTER(Tuning), P]),
         "eh_batch_build": (I, [U32, P, U64, P, P, I, P, C.POINTER(P)]),
         "eh_batch_count": (I, [P, U32, P, P]),
@@ -437,9 +438,13 @@ class Matrix:
         check(load().eh_list_triangles(self.h, C.c_void_p(d_out), capacity, C.c_void_p(d_total),
                                        _stream(stream)))
 
-    def tune(self, stream=None):
+    def tune(self, stream=None, counts_per_build=0):
+        """eh_matrix_tune, or eh_matrix_tune_for when counts_per_build > 0."""
         t = Tuning()
-        check(load().eh_matrix_tune(self.h, _stream(stream), C.byref(t)))
+        if counts_per_build:
+            check(load().eh_matrix_tune_for(self.h, counts_per_build, _stream(stream), C.byref(t)))
+        else:
+            check(load().eh_matrix_tune(self.h, _stream(stream), C.byref(t)))
         return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
     def set_shape(self, light_max, unit_span, ctas_per_sm, core_rows, core_hot_words=0, core_filter_words=0,

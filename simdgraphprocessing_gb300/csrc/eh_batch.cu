@@ -16,6 +16,7 @@
 // layout, size bucket) in the process and optionally in a file named by the
 // EH_TUNE_CACHE environment variable.
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -108,7 +109,28 @@ eh_status apply_shape(Matrix* m, const Shape& s, cudaStream_t st) {
   m->core_hot_words = s.hot;
   m->core_filter_words = s.filter;
   m->grid = sms * (int)s.ctas;
+  m->shape_set = true;
   return ensure_plan(m, st);
+}
+
+// Host time of building the current shape's own plan parts from nothing (heavy
+// units, dense core, row filters), as a matrix built for a few counts pays
+// them: median of 3.
+eh_status time_setup(Matrix* m, cudaStream_t st, float* ms) {
+  std::vector<float> t;
+  for (int r = 0; r < 3; r++) {
+    eh_status s = drop_shape_parts(m, st);
+    if (s == EH_OK && cudaStreamSynchronize(st) != cudaSuccess) s = set_error(EH_ERR_CUDA, "plan parts free");
+    if (s != EH_OK) return s;
+    const auto t0 = std::chrono::steady_clock::now();
+    s = ensure_plan(m, st);
+    if (s == EH_OK && cudaStreamSynchronize(st) != cudaSuccess) s = set_error(EH_ERR_CUDA, "plan parts build");
+    if (s != EH_OK) return s;
+    t.push_back(std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  }
+  std::sort(t.begin(), t.end());
+  *ms = t[t.size() / 2];
+  return EH_OK;
 }
 
 // Median of `reps` timed triangle counts (after one warm-up) for the matrix's current shape;
@@ -142,14 +164,19 @@ eh_status time_shape(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs,
   return EH_OK;
 }
 
-eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaStream_t st, eh_tuning* res) {
+// per_build = 0 ranks shapes by the count's time alone (a matrix counted many
+// times); per_build = k by the count's time plus the shape's one-shot plan
+// cost (time_setup) / k (a matrix built for k counts).
+eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaStream_t st, eh_tuning* res,
+               uint32_t per_build) {
   // The first plan build looks up the shape cache itself (apply_cached_shape), so
   // it runs before this function takes the cache lock.
   eh_status s = ensure_plan(m, st);
   if (s != EH_OK) return s;
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   load_tune_file();
-  const std::string key = tune_key(m, graph_rows != nullptr);
+  std::string key = tune_key(m, graph_rows != nullptr);
+  if (per_build) key += "|per_build" + std::to_string(per_build);
   unsigned long long* out = nullptr;
   const size_t outn = graph_rows ? num_graphs : 1;
   if (pool_alloc((void**)&out, outn * sizeof(unsigned long long), st) != cudaSuccess)
@@ -157,8 +184,16 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
   auto it = g_tune_cache.find(key);
   Shape best{m->light_max, m->unit_span, (uint32_t)max_ctas_per_sm(m->device), m->core_limit, m->core_hot_words,
              m->core_filter_words};
-  float best_ms = 0;
+  float best_ms = 0, best_score = 0;
   uint32_t tried = 0;
+  // Count time of the current shape, and its rank (count time plus the
+  // amortised one-shot plan cost when per_build is set).
+  auto measure = [&](float* ms, float* score) {
+    s = time_shape(m, graph_rows, num_graphs, out, st, 3, ms);
+    *score = *ms;
+    float setup = 0;
+    if (s == EH_OK && per_build && (s = time_setup(m, st, &setup)) == EH_OK) *score += setup / (float)per_build;
+  };
   if (it != g_tune_cache.end()) {
     best = it->second;
     s = apply_shape(m, best, st);
@@ -167,16 +202,17 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
   } else {
     const int cmax = max_ctas_per_sm(m->device);
     s = apply_shape(m, best, st);
-    if (s == EH_OK) s = time_shape(m, graph_rows, num_graphs, out, st, 3, &best_ms);
+    if (s == EH_OK) measure(&best_ms, &best_score);
     tried = 1;
     auto consider = [&](Shape c) {
       if (s != EH_OK) return;
       s = apply_shape(m, c, st);
-      float ms = 0;
-      if (s == EH_OK) s = time_shape(m, graph_rows, num_graphs, out, st, 3, &ms);
+      float ms = 0, score = 0;
+      if (s == EH_OK) measure(&ms, &score);
       tried++;
-      if (s == EH_OK && ms < best_ms) {
+      if (s == EH_OK && score < best_score) {
         best_ms = ms;
+        best_score = score;
         best = c;
       }
     };
@@ -262,7 +298,17 @@ eh_status eh_matrix_tune(eh_matrix_t mh, void* stream, eh_tuning* result) {
   if (m->selection == EH_SELECT_MASK)
     return set_error(EH_ERR_UNSUPPORTED,
                      "tuning times the triangle count (EH_SELECT_LOWER) or the lollipop count (EH_SELECT_ALL)");
-  return eh::tune(m, nullptr, 0, reinterpret_cast<cudaStream_t>(stream), result);
+  return eh::tune(m, nullptr, 0, reinterpret_cast<cudaStream_t>(stream), result, 0);
+}
+
+eh_status eh_matrix_tune_for(eh_matrix_t mh, uint32_t counts_per_build, void* stream, eh_tuning* result) {
+  if (!mh) return set_error(EH_ERR_INVALID_ARGUMENT, "matrix is NULL");
+  eh::Matrix* m = reinterpret_cast<eh::Matrix*>(mh);
+  cudaSetDevice(m->device);
+  if (m->selection == EH_SELECT_MASK)
+    return set_error(EH_ERR_UNSUPPORTED,
+                     "tuning times the triangle count (EH_SELECT_LOWER) or the lollipop count (EH_SELECT_ALL)");
+  return eh::tune(m, nullptr, 0, reinterpret_cast<cudaStream_t>(stream), result, counts_per_build);
 }
 
 eh_status eh_matrix_set_shape(eh_matrix_t mh, const eh_tuning* shape, void* stream) {
@@ -400,7 +446,7 @@ eh_status eh_batch_tune(eh_batch_t bh, void* stream, eh_tuning* result) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
   }
-  return eh::tune(b->m, b->d_graph_rows, b->num_graphs, reinterpret_cast<cudaStream_t>(stream), result);
+  return eh::tune(b->m, b->d_graph_rows, b->num_graphs, reinterpret_cast<cudaStream_t>(stream), result, 0);
 }
 
 void eh_batch_free(eh_batch_t bh) {

@@ -440,7 +440,93 @@ __device__ void write_pshort(uint16_t* s, uint64_t row, uint64_t b, uint64_t e, 
   s[size_pos] = (uint16_t)plen;
 }
 
-__global__ void __launch_bounds__(kBlock) k_encode(uint64_t n, const uint64_t* __restrict__ off,
+// Warp-parallel form of write_pshort over a slice nbr[s0, s1) of a row.  In
+// the payload, the selected element of rank s (0-based among the row's
+// selected elements) in partition P (0-based) sits at u16 position
+// s + 2 (P + 1), and partition P's header [hi][count - 1] at f_P + 2 P, where
+// f_P is the rank of its first element.  So each element finds its slot from
+// two warp prefix counts (selected elements and partition starts before it); a
+// partition's first element writes its header's hi and the size of the
+// partition before it (its own rank minus that partition's first rank, minus
+// one).  `c` carries the row's state into the slice (rank of its first
+// selected element, index of the open partition or -1, that partition's first
+// rank and high half); the returned carry continues after the slice.  The
+// size of the row's last partition is left to the caller.
+struct PshortCarry {
+  uint64_t s;           // rank of the next selected element
+  int32_t part;         // partition of the last selected element so far (-1: none)
+  uint64_t open_first;  // rank of that partition's first element
+  uint32_t hi;          // its high half
+};
+__device__ PshortCarry warp_write_pshort(uint16_t* out, uint64_t row, uint64_t s0, uint64_t s1,
+                                         const uint32_t* __restrict__ nbr, const uint8_t* __restrict__ mask,
+                                         int sel, uint32_t lane, PshortCarry c) {
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint64_t base = s0; base < s1; base += 32) {
+    const uint64_t k = base + lane;
+    const bool valid = k < s1;
+    const uint32_t x = valid ? nbr[k] : 0u;
+    const bool take = valid && is_selected(sel, x, row, mask, k);
+    const uint32_t bal = __ballot_sync(FULL, take);
+    if (!bal) continue;
+    const uint32_t hi = x >> 16;
+    const uint32_t below = bal & lt;
+    const uint32_t ph = __shfl_sync(FULL, hi, below ? 31 - __clz(below) : lane);
+    const bool first = take && (below ? ph != hi : (c.part < 0 || c.hi != hi));
+    const uint32_t fbal = __ballot_sync(FULL, first);
+    const uint64_t rank = c.s + __popc(below);
+    const int32_t part = c.part + (int32_t)__popc(fbal & (lt | (1u << lane)));
+    const uint32_t fbelow = fbal & lt;
+    const uint64_t fr = __shfl_sync(FULL, rank, fbelow ? 31 - __clz(fbelow) : lane);
+    if (take) out[rank + 2 * (uint64_t)(part + 1)] = (uint16_t)(x & 0xffffu);
+    if (first) {
+      out[rank + 2 * (uint64_t)part] = (uint16_t)hi;
+      if (part > 0) {
+        const uint64_t pf = fbelow ? fr : c.open_first;  // first rank of partition part - 1
+        out[pf + 2 * (uint64_t)(part - 1) + 1] = (uint16_t)(rank - pf - 1);
+      }
+    }
+    const uint32_t top = 31 - __clz(bal);
+    c.hi = __shfl_sync(FULL, hi, top);
+    if (fbal) c.open_first = __shfl_sync(FULL, rank, 31 - __clz(fbal));
+    c.s += __popc(bal);
+    c.part += (int32_t)__popc(fbal);
+  }
+  return c;
+}
+
+// Per-slice summary for the CTA form: selected elements, partition starts
+// counted as if the slice began a row, the first and last high halves, and the
+// slice-local rank of its last such start.
+struct PshortSlice {
+  uint32_t cnt, starts, first_hi, last_hi, last_start;
+};
+__device__ PshortSlice warp_scan_pshort(uint64_t row, uint64_t s0, uint64_t s1, const uint32_t* __restrict__ nbr,
+                                        const uint8_t* __restrict__ mask, int sel, uint32_t lane) {
+  PshortSlice r{0, 0, 0, 0, 0};
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint64_t base = s0; base < s1; base += 32) {
+    const uint64_t k = base + lane;
+    const bool valid = k < s1;
+    const uint32_t x = valid ? nbr[k] : 0u;
+    const bool take = valid && is_selected(sel, x, row, mask, k);
+    const uint32_t bal = __ballot_sync(FULL, take);
+    if (!bal) continue;
+    const uint32_t hi = x >> 16;
+    const uint32_t below = bal & lt;
+    const uint32_t ph = __shfl_sync(FULL, hi, below ? 31 - __clz(below) : lane);
+    const bool first = take && (below ? ph != hi : (r.cnt == 0 || r.last_hi != hi));
+    const uint32_t fbal = __ballot_sync(FULL, first);
+    if (r.cnt == 0) r.first_hi = __shfl_sync(FULL, hi, __ffs(bal) - 1);
+    if (fbal) r.last_start = r.cnt + __popc(bal & ((1u << (31 - __clz(fbal))) - 1u));
+    r.last_hi = __shfl_sync(FULL, hi, 31 - __clz(bal));
+    r.cnt += __popc(bal);
+    r.starts += __popc(fbal);
+  }
+  return r;
+}
+
+__global__ void __launch_bounds__(kBlock, 6) k_encode(uint64_t n, const uint64_t* __restrict__ off,
                                                    const uint32_t* __restrict__ nbr,
                                                    const uint8_t* __restrict__ mask, int sel,
                                                    const RowMeasure* __restrict__ meas,
@@ -494,7 +580,9 @@ __global__ void __launch_bounds__(kBlock) k_encode(uint64_t n, const uint64_t* _
       if (e - b > kBigRow) continue;
       uint4* dst = arena + __shfl_sync(FULL, my_o, q);
       if (type == TY_PSHORT) {
-        if (lane == 0) write_pshort(reinterpret_cast<uint16_t*>(dst), row, b, e, nbr, mask, sel);
+        uint16_t* out = reinterpret_cast<uint16_t*>(dst);
+        const PshortCarry c = warp_write_pshort(out, row, b, e, nbr, mask, sel, lane, PshortCarry{0, -1, 0, 0});
+        if (lane == 0 && c.part >= 0) out[c.open_first + 2 * (uint64_t)c.part + 1] = (uint16_t)(c.s - c.open_first - 1);
         continue;
       }
       uint32_t k_sel = 0;
@@ -531,6 +619,8 @@ __global__ void __launch_bounds__(kBigBlock) k_encode_big(const uint64_t* __rest
                                                           const uint32_t* __restrict__ n_big) {
   constexpr int NWB = kBigBlock / 32;
   __shared__ uint32_t s_cnt[NWB];
+  __shared__ PshortSlice s_ps[NWB];
+  __shared__ PshortCarry s_carry[NWB];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nb = *n_big;
   for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
@@ -540,12 +630,34 @@ __global__ void __launch_bounds__(kBigBlock) k_encode_big(const uint64_t* __rest
     if (m.card == 0) continue;
     const uint64_t b = off[row], e = off[row + 1];
     uint4* dst = arena + off16[row];
-    if (type == TY_PSHORT) {
-      if (threadIdx.x == 0) write_pshort(reinterpret_cast<uint16_t*>(dst), row, b, e, nbr, mask, sel);
-      continue;
-    }
     const uint64_t slice = ((e - b + NWB - 1) / NWB + 31) & ~31ull;
     const uint64_t s0 = min(e, b + warp * slice), s1 = min(e, s0 + slice);
+    if (type == TY_PSHORT) {
+      // Each warp summarises its slice, one thread chains the summaries into
+      // each slice's carry-in, then every warp writes its slice.
+      uint16_t* out = reinterpret_cast<uint16_t*>(dst);
+      const PshortSlice ps = warp_scan_pshort(row, s0, s1, nbr, mask, sel, lane);
+      if (lane == 0) s_ps[warp] = ps;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        PshortCarry c{0, -1, 0, 0};
+        for (int w = 0; w < NWB; w++) {
+          s_carry[w] = c;
+          const PshortSlice& q = s_ps[w];
+          if (q.cnt == 0) continue;
+          const uint32_t joins = (c.part >= 0 && c.hi == q.first_hi) ? 1u : 0u;  // slice continues the open partition
+          if (q.starts > joins) c.open_first = c.s + q.last_start;
+          c.part += (int32_t)(q.starts - joins);
+          c.s += q.cnt;
+          c.hi = q.last_hi;
+        }
+        if (c.part >= 0) out[c.open_first + 2 * (uint64_t)c.part + 1] = (uint16_t)(c.s - c.open_first - 1);
+      }
+      __syncthreads();
+      warp_write_pshort(out, row, s0, s1, nbr, mask, sel, lane, s_carry[warp]);
+      __syncthreads();  // s_ps / s_carry are rewritten for the next row
+      continue;
+    }
     if (type == TY_BITSET) {
       unsigned long long* words = reinterpret_cast<unsigned long long*>(dst);
       for (uint64_t k = s0 + lane; k < s1; k += 32) {

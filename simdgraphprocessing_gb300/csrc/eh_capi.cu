@@ -318,12 +318,39 @@ eh_status ensure_core(Matrix* m, cudaStream_t st) {
   return EH_OK;
 }
 
+eh_status drop_shape_parts(Matrix* m, cudaStream_t st) {
+  Plan& p = m->plan;
+  if (!p.units && !p.core && !p.filter) return EH_OK;
+  CU(wait_uses(m, st), "plan parts");  // launches on other streams may still read them
+  if (p.units) {
+    CU(cudaFreeAsync(p.units, st), "units");
+    m->device_bytes -= p.units_cap * sizeof(uint2);
+    p.units = nullptr;
+    p.units_cap = 0;
+    p.n_units = 0;
+  }
+  if (p.filter) {
+    CU(cudaFreeAsync(p.filter, st), "row filters");
+    m->device_bytes -= (uint64_t)(p.filter_k - kFilterLo) * p.filter_words * 8;
+    p.filter = nullptr;
+    p.filter_words = 0;
+    p.filter_k = 0;
+  }
+  if (p.core) {
+    CU(cudaFreeAsync(p.core, st), "core");
+    m->device_bytes -= core_row_offset(p.core_k) * 8;
+    p.core = nullptr;
+    p.core_k = 0;
+  }
+  return EH_OK;
+}
+
 // Row order (descending card) and decoded copies of the giant non-uint pivots,
 // then the heavy units for the matrix's current work shape.
 eh_status ensure_plan(Matrix* m, cudaStream_t st) {
   Plan& p = m->plan;
   if (!p.ready) {
-    apply_cached_shape(m);
+    if (!m->shape_set) apply_cached_shape(m);
     uint32_t* hist = nullptr;
     uint32_t* cursor = nullptr;
     const uint64_t nn = m->n ? m->n : 1;

@@ -73,6 +73,7 @@ struct Matrix {
   uint32_t core_hot_words = 0;          // see PivotArgs::core_hot_words
   uint32_t core_filter_words = 0;       // words per core row filter (0: no filters)
   bool is_batch = false;            // the union matrix of an eh_batch_t
+  bool shape_set = false;           // a shape was given (eh_matrix_set_shape, the tuner): no cached shape
   // Where the matrix's buffers are read: one event per stream, recorded after
   // every launch that reads them (not while that stream is being captured).
   // Freeing or replacing a buffer makes the freeing stream wait for these
@@ -113,6 +114,9 @@ eh_status build_device(uint64_t n, const uint64_t* d_off, const uint32_t* d_nbr,
 eh_status ensure_plan(Matrix* m, cudaStream_t st);
 eh_status ensure_units(Matrix* m, uint32_t light_max, uint32_t unit_span, cudaStream_t st);
 eh_status ensure_core(Matrix* m, cudaStream_t st);
+// Frees the parts of the plan that depend on the work shape (heavy units, dense
+// core, row filters), so that the next ensure_plan builds them from nothing.
+eh_status drop_shape_parts(Matrix* m, cudaStream_t st);
 // Records that launches reading m's buffers were just queued on st.
 void note_use(Matrix* m, cudaStream_t st);
 // Makes st wait for every launch note_use has recorded on m, on any stream.

@@ -92,3 +92,26 @@ def test_full_row_matrix_tunes_on_lollipops(eh, oracle):
     shape = m.tune()
     assert shape["configs_tried"] >= 1
     assert m.count_lollipops() == want
+
+
+@pytest.mark.timeout(300)
+def test_one_shot_tuning_and_explicit_shape(eh, oracle):
+    """eh_matrix_tune_for ranks shapes with their one-shot plan cost; its shape,
+    given to a fresh matrix with eh_matrix_set_shape, is not replaced by the
+    cached shape of eh_matrix_tune when the plan is built (seen in the dense
+    core's memory), and counts stay exact."""
+    off, nbr = eh.graph("rmat", 15, scale=13, edges=80000).csr()[:2]
+    want = oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.HYBRID).triangles()
+    m = eh.Matrix.build(off, nbr, "lower", "hybrid")
+    once = m.tune(counts_per_build=1)
+    assert once["configs_tried"] >= 1 and m.count_triangles() == want
+    many = m.tune()
+    assert m.count_triangles() == want
+    sizes = {}
+    for core in (0, 8192):
+        fresh = eh.Matrix.build(off, nbr, "lower", "hybrid")
+        fresh.set_shape(once["light_max"], once["unit_span"], once["ctas_per_sm"], core)
+        assert fresh.count_triangles() == want
+        sizes[core] = fresh.info()["device_bytes"]
+    assert sizes[8192] - sizes[0] >= 8192 * 8191 // 128  # the 8,192-row core is there, whatever the cache says
+    assert many["configs_tried"] >= 1

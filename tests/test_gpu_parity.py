@@ -95,6 +95,28 @@ def test_intersect_rows_all_layout_pairs(eh, oracle):
         assert np.array_equal(got, o.intersect_rows(a, b)), layout
 
 
+@pytest.mark.parametrize("selection", ["all", "lower", "mask"])
+def test_pshort_rows_over_several_partitions(eh, oracle, selection):
+    """pshort payloads written by a warp or a CTA at once (rows over 32 and
+    over 4,096 entries) equal the reference encoder's bytes when rows span
+    several 2^16 partitions, partitions cross the warps' slices, and a mask
+    drops elements anywhere in a row."""
+    off, nbr = eh.graph("rmat", 25, scale=18, edges=3000000).csr()[:2]
+    mask = None
+    if selection == "mask":
+        mask = (np.random.default_rng(5).random(len(nbr)) < 0.7).astype(np.uint8)
+    m = eh.Matrix.build(off, nbr, selection=selection, layout="pshort", mask=mask)
+    o = oracle.Matrix(off, nbr, oracle.SELECTIONS[selection], oracle.PSHORT, mask=mask)
+    t, c, b = m.row_meta()
+    ot, oc, ob = o.row_meta()
+    assert np.array_equal(c, oc) and np.array_equal(b, ob)
+    assert c.max() > (4096 if selection != "lower" else 256)  # pruned hub rows are short
+    rng = np.random.default_rng(7)
+    rows = np.concatenate([np.argsort(-c.astype(np.int64))[:60], rng.integers(0, len(c), 200)])
+    for r in rows:
+        assert m.export_row(int(r)) == o.row_bytes(int(r)), int(r)
+
+
 def test_rejects_unsorted_rows_without_fault(eh):
     off = np.array([0, 2, 4, 6], np.uint64)
     nbr = np.array([2, 1, 0, 2, 0, 1], np.uint32)  # row 0 descending
