@@ -373,7 +373,11 @@ def run_ours(a, rank, world, local_rank):
                          % (count, fx0["counts"]["triangles"], fx0["name"]))
     value, ms_max = aggregate(pruned, ms, world, "cuda")
 
-    # End to end through the C ABI from pinned host buffers.
+    # End to end through the C ABI from pinned host buffers.  The passes stand
+    # alone: the resident matrix of the timed counts (and its dense core) is
+    # released first.
+    del m
+    torch.cuda.synchronize()
     e2e = None
     if not a.no_e2e and not a.profile:
         h_off = torch.from_numpy(off.view("int64")).pin_memory()
