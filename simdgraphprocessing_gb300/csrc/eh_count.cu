@@ -239,9 +239,20 @@ __global__ void __launch_bounds__(kCtaThreads, 6) k_pivots_heavy(PivotArgs a, co
   cta_add(acc, a);
 }
 
+// Word x / 64 of core row j.  With core_hot_words set, words near the start of
+// each core row (the highest-degree columns, where most probes land) keep
+// their L2 lines and the others are evicted first.
+template <bool HOT>
+__device__ __forceinline__ unsigned long long core_word(const PivotArgs& a, uint32_t j, uint32_t x) {
+  const unsigned long long* p = a.core + core_row_offset(j) + (x >> 6);
+  if (!HOT) return __ldg(p);
+  return (x >> 6) < a.core_hot_words ? ld_keep(p) : ld_stream(p);
+}
+
 // Light pivots: 8 resident CTAs per SM (64 warps, 32 registers per thread):
-// bound by the latency of scattered probes, so occupancy pays.
-template <bool LOLLI>
+// bound by the latency of scattered probes, so occupancy and two probes in
+// flight per lane pay.
+template <bool LOLLI, bool HOT>  // HOT: core_hot_words != 0
 __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
   __shared__ uint32_t wlist[NWARPS][kLightMax];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -266,29 +277,33 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
       uint32_t e = 1, t = lane;
       while (t >= e) { t -= e; e++; }
       uint32_t cnt = 0;
-      for (uint32_t q = lane; q < pairs; q += 32) {
-        const uint32_t j = list[e], x = list[t];
-        // The row's filter first (if it has one): a clear bit means x is not
-        // in row(j), and neither the core word nor the row is read.
-        bool maybe = true;
-        if (j >= kFilterLo && j < a.filter_k) {
-          const uint32_t b = filter_bit(x, a.filter_words);
-          maybe = (ld_keep(a.filter + (uint64_t)(j - kFilterLo) * a.filter_words + (b >> 6)) >> (b & 63)) & 1ull;
-        }
-        if (maybe && j < a.core_k) {  // x < j: one word of the core row j
-          // With core_hot_words set, words near the start of each core row
-          // (the highest-degree columns, where most probes land) keep their
-          // L2 lines and the others are evicted first.
-          const unsigned long long* p = a.core + core_row_offset(j) + (x >> 6);
-          const uint32_t hot = a.core_hot_words;
-          const unsigned long long w = hot == 0 ? __ldg(p) : (x >> 6) < hot ? ld_keep(p) : ld_stream(p);
-          cnt += (uint32_t)((w >> (x & 63)) & 1ull);
-        } else if (maybe) {
-          const RowView B = load_view(a.desc, a.arena, j);
-          cnt += row_contains(B, x);
-        }
+      // Two pairs per lane and step (q and q + 32), each probed the same way:
+      // the row's filter word first (if the row has a filter; a clear bit means
+      // x is not in row(j)), then one word of the core row j when j < core_k,
+      // else the row itself.  Both pairs' loads are issued before either
+      // result is used, so two probe chains are in flight per lane.
+      for (uint32_t q = lane; q < pairs; q += 64) {
+        const uint32_t j0 = list[e], x0 = list[t];
         t += 32;
         while (t >= e && e < c) { t -= e; e++; }
+        const bool two = q + 32 < pairs;
+        const uint32_t j1 = two ? list[e] : 0u, x1 = two ? list[t] : 0u;
+        t += 32;
+        while (t >= e && e < c) { t -= e; e++; }
+        const uint32_t b0 = filter_bit(x0, a.filter_words), b1 = filter_bit(x1, a.filter_words);
+        const unsigned long long f0 = (j0 >= kFilterLo && j0 < a.filter_k)
+                                          ? ld_keep(a.filter + (uint64_t)(j0 - kFilterLo) * a.filter_words + (b0 >> 6))
+                                          : ~0ull;
+        const unsigned long long f1 = (two && j1 >= kFilterLo && j1 < a.filter_k)
+                                          ? ld_keep(a.filter + (uint64_t)(j1 - kFilterLo) * a.filter_words + (b1 >> 6))
+                                          : ~0ull;
+        const bool m0 = (f0 >> (b0 & 63)) & 1ull, m1 = two && ((f1 >> (b1 & 63)) & 1ull);
+        const bool c0 = m0 && j0 < a.core_k, c1 = m1 && j1 < a.core_k;
+        const unsigned long long v0 = c0 ? core_word<HOT>(a, j0, x0) : 0ull;
+        const unsigned long long v1 = c1 ? core_word<HOT>(a, j1, x1) : 0ull;
+        cnt += (uint32_t)((v0 >> (x0 & 63)) & 1ull) + (uint32_t)((v1 >> (x1 & 63)) & 1ull);
+        if (m0 && !c0) cnt += row_contains(load_view(a.desc, a.arena, j0), x0);
+        if (m1 && !c1) cnt += row_contains(load_view(a.desc, a.arena, j1), x1);
       }
       unsigned long long pc = LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
       if (a.graph_rows) {  // batch: one atomic per pivot into its graph's count
@@ -417,7 +432,7 @@ static int grid_of(int device, bool heavy) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (heavy) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pivots_heavy<false>, kCtaThreads, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pivots_light<false>, kCtaThreads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pivots_light<false, false>, kCtaThreads, 0);
   g = std::max(1, sms) * std::max(1, per);
   cache[device][heavy].store(g);
   return g;
@@ -438,7 +453,10 @@ static cudaError_t launch_pivots(const PivotArgs& a, const uint2* units, uint32_
     const int gh = std::min(grid, grid_of(device, true));
     k_pivots_heavy<LOLLI><<<std::max(gh, 1), kCtaThreads, 0, st>>>(a, units, n_units);
   }
-  if (a.n_order > a.n_heavy) k_pivots_light<LOLLI><<<std::max(grid, 1), kCtaThreads, 0, st>>>(a);
+  if (a.n_order > a.n_heavy) {
+    if (a.core_hot_words) k_pivots_light<LOLLI, true><<<std::max(grid, 1), kCtaThreads, 0, st>>>(a);
+    else k_pivots_light<LOLLI, false><<<std::max(grid, 1), kCtaThreads, 0, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
