@@ -382,7 +382,7 @@ def run_ours(a, rank, world, local_rank):
     if not a.no_e2e and not a.profile:
         h_off = torch.from_numpy(off.view("int64")).pin_memory()
         h_nbr = torch.from_numpy(nbr.view("int32")).pin_memory()
-        e2e_times = []
+        e2e_times, e2e_phases = [], []
         t1 = eh.Tuning(**{k: shape1[k] for k in ("light_max", "unit_span", "ctas_per_sm", "core_rows",
                                                  "core_hot_words", "core_filter_words")})
         torch.cuda.synchronize()
@@ -393,7 +393,9 @@ def run_ours(a, rank, world, local_rank):
             h = C.c_void_p()
             eh.check(L.eh_matrix_build(len(off) - 1, C.c_void_p(h_off.data_ptr()), C.c_void_p(h_nbr.data_ptr()),
                                        None, eh.SELECT_LOWER, eh.LAYOUTS[a.layout], st, C.byref(h)))
+            tb = time.perf_counter()  # each call below returns after its work is done
             eh.check(L.eh_matrix_set_shape(h, C.byref(t1), st))
+            tp = time.perf_counter()
             c = C.c_uint64()
             eh.check(L.eh_count_triangles(h, C.byref(c), st))
             dt = time.perf_counter() - t
@@ -402,13 +404,17 @@ def run_ours(a, rank, world, local_rank):
                 raise SystemExit("e2e count mismatch %d vs %d" % (c.value, count_ref))
             if k > 0:  # the first pass maps the library's memory pool
                 e2e_times.append(dt)
+                e2e_phases.append((tb - t, tp - tb, t + dt - tp))
         e2e_value, e2e_ms = aggregate(pruned, 1e3 * statistics.mean(e2e_times), world, "cuda")
         e2e = {"value": e2e_value, "unit": "edges/s",
                "h2d_bytes_per_step": int(off.nbytes + nbr.nbytes), "d2h_bytes_per_step": 8,
                "ms_per_step": e2e_ms, "steps": len(e2e_times),
                "includes": "pinned H2D of the full symmetric CSR, device select/optimize/encode/plan, "
                            "triangle count, u64 result D2H",
-               "work_shape": shape1}
+               "work_shape": shape1,
+               "step_ms": [round(1e3 * x, 3) for x in e2e_times],
+               "phase_ms_median": {k: round(1e3 * statistics.median(p[i] for p in e2e_phases), 3)
+                                   for i, k in enumerate(("build", "plan", "count"))}}
 
     if rank != 0:
         if dist:

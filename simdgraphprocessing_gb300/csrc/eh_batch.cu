@@ -239,7 +239,7 @@ eh_status tune(Matrix* m, const uint32_t* graph_rows, uint32_t num_graphs, cudaS
         consider(Shape{after_core.light_max, after_core.unit_span, (uint32_t)c, after_core.core, after_core.hot,
                          after_core.filter});
     const Shape after_ctas = best;
-    for (uint32_t lm : {32u, 64u, 96u})
+    for (uint32_t lm : {32u, 64u, 96u, 128u, 160u})
       if (lm != after_ctas.light_max && lm <= kLightMax)
         consider(Shape{lm, after_ctas.unit_span, after_ctas.ctas, after_ctas.core, after_ctas.hot, after_ctas.filter});
     const Shape after_lm = best;

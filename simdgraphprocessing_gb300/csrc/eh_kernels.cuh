@@ -93,7 +93,7 @@ struct PivotArgs {
   uint32_t filter_k;
 };
 constexpr uint32_t kCtaThreads = 256;
-constexpr uint32_t kLightMax = 96;     // largest light_max: warp-wide pivots fit a slice of this size
+constexpr uint32_t kLightMax = 160;    // largest light_max: warp-wide pivots fit a slice of this size
 constexpr uint32_t kDefaultLightMax = 96;
 constexpr uint32_t kDefaultUnitSpan = 128;
 constexpr uint32_t kCtaListCap = 2048; // CTA-staged list capacity (elements)

@@ -79,7 +79,7 @@ def test_single_matrix_tuning_keeps_counts(eh, oracle):
     m = eh.Matrix.build(off, nbr, "lower", "hybrid")
     want = m.count_triangles()
     shape = m.tune()
-    assert shape["light_max"] in (32, 64, 96) and shape["unit_span"] in (32, 64, 128, 256, 512, 1024, 2048)
+    assert shape["light_max"] in (32, 64, 96, 128, 160) and shape["unit_span"] in (32, 64, 128, 256, 512, 1024, 2048)
     assert m.count_triangles() == want
     assert m.count_cliques(4) == oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.HYBRID).cliques(4)
 
