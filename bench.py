@@ -10,7 +10,8 @@ u32 ids, u64 count.
 One step = one triangle-count pass over the encoded graph.  `value` is pruned
 edges per second with the encoded graph resident in HBM (count phase only, as
 the reference's own "Time[UNDIRECTED TRIANGLE COUNTING]" timer measures).
-`e2e` runs the same pass through the C ABI from pinned host CSR buffers: upload,
+`e2e` (the median of its timed passes) runs the same pass through the C ABI
+from pinned host CSR buffers: upload,
 device select/optimize/encode, the plan with the work shape tuned for a matrix
 built and counted once (eh_matrix_tune_for, counts_per_build = 1), count, and
 the u64 result copied back.  `value` uses the shape tuned for a resident matrix
@@ -386,7 +387,8 @@ def run_ours(a, rank, world, local_rank):
         t1 = eh.Tuning(**{k: shape1[k] for k in ("light_max", "unit_span", "ctas_per_sm", "core_rows",
                                                  "core_hot_words", "core_filter_words")})
         torch.cuda.synchronize()
-        for k in range(a.e2e_steps + 1):
+        e2e_warm = 2  # untimed passes: the first maps the library's memory pools
+        for k in range(a.e2e_steps + e2e_warm):
             flush.fill_(k & 0xff)
             torch.cuda.synchronize()
             t = time.perf_counter()
@@ -402,17 +404,22 @@ def run_ours(a, rank, world, local_rank):
             L.eh_matrix_free(h)  # outside the timed region, as a caller frees a matrix it is done with
             if c.value != count_ref:
                 raise SystemExit("e2e count mismatch %d vs %d" % (c.value, count_ref))
-            if k > 0:  # the first pass maps the library's memory pool
+            if k >= e2e_warm:
                 e2e_times.append(dt)
                 e2e_phases.append((tb - t, tp - tb, t + dt - tp))
-        e2e_value, e2e_ms = aggregate(pruned, 1e3 * statistics.mean(e2e_times), world, "cuda")
+        # The median pass: on a box whose previous job has just ended, the first
+        # passes of a process have been seen to take up to 20x longer (host or
+        # driver work outside this process); every pass is listed in step_ms.
+        e2e_value, e2e_ms = aggregate(pruned, 1e3 * statistics.median(e2e_times), world, "cuda")
         e2e = {"value": e2e_value, "unit": "edges/s",
                "h2d_bytes_per_step": int(off.nbytes + nbr.nbytes), "d2h_bytes_per_step": 8,
-               "ms_per_step": e2e_ms, "steps": len(e2e_times),
+               "ms_per_step": e2e_ms, "steps": len(e2e_times), "statistic": "median of the timed passes",
+               "mean_ms": 1e3 * statistics.mean(e2e_times),
                "includes": "pinned H2D of the full symmetric CSR, device select/optimize/encode/plan, "
                            "triangle count, u64 result D2H",
                "work_shape": shape1,
                "step_ms": [round(1e3 * x, 3) for x in e2e_times],
+               "step_phase_ms": [[round(1e3 * x, 3) for x in p] for p in e2e_phases],
                "phase_ms_median": {k: round(1e3 * statistics.median(p[i] for p in e2e_phases), 3)
                                    for i, k in enumerate(("build", "plan", "count"))}}
 

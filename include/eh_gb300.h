@@ -198,8 +198,10 @@ eh_status eh_matrix_get_max_row_id(eh_matrix_t m, uint32_t* row);
 /* Algorithmic bytes of one triangle-count pass:
  * sum_i [8 + bytes(A_i)] + sum_{(i,j) selected} bytes(B_j), bytes = layout payload. */
 eh_status eh_matrix_triangle_bytes(eh_matrix_t m, uint64_t* bytes);
-/* Waits for the device, then returns the matrix's memory to the library's
- * pool (which keeps up to 16 GiB of freed memory mapped per device). */
+/* Returns the matrix's memory to the library's pools (each keeps up to 16 GiB
+ * of freed memory mapped per device), stream-ordered: once every launch the
+ * library made on the matrix, on any stream, has finished; the host and
+ * unrelated streams do not wait. */
 void eh_matrix_free(eh_matrix_t m);
 
 /* ------------------------------------------------------------------------- */
@@ -349,8 +351,8 @@ typedef struct eh_server* eh_server_t;
 typedef struct eh_server_config {
   uint32_t slots;          /* concurrent queries on the device (1..64)            */
   uint64_t hbm_cap_bytes;  /* resident matrices + query scratch never exceed this
-                            * (the library's pool may keep up to 16 GiB of freed
-                            * memory mapped on top of it)                        */
+                            * (the library's two pools may each keep up to
+                            * 16 GiB of freed memory mapped on top of it)        */
 } eh_server_config;
 typedef enum eh_query_kind {
   EH_QUERY_TRIANGLES = 0,     /* param unused                                    */

@@ -40,11 +40,11 @@ static uint64_t flattened_bytes(int layout, const RowDesc& d) {
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_device_mu;
-cudaMemPool_t g_pool[kMaxDevices] = {};
+cudaMemPool_t g_pool[kMaxDevices][2] = {};
 cudaStream_t g_upload_stream[kMaxDevices] = {};
 }  // namespace
 
-cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st) {
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st, PoolKind kind) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -52,7 +52,7 @@ cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st) {
   cudaMemPool_t pool;
   {
     std::lock_guard<std::mutex> g(g_device_mu);
-    if (!g_pool[dev]) {
+    if (!g_pool[dev][kind]) {
       cudaMemPoolProps props = {};
       props.allocType = cudaMemAllocationTypePinned;
       props.location.type = cudaMemLocationTypeDevice;
@@ -64,9 +64,9 @@ cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st) {
         cudaMemPoolDestroy(created);
         return e;
       }
-      g_pool[dev] = created;
+      g_pool[dev][kind] = created;
     }
-    pool = g_pool[dev];
+    pool = g_pool[dev][kind];
   }
   return cudaMallocFromPoolAsync(p, bytes, pool, st);
 }
@@ -301,14 +301,14 @@ eh_status ensure_core(Matrix* m, cudaStream_t st) {
   }
   if (want && !p.core) {
     const uint64_t words = core_row_offset(want);
-    CU(pool_alloc((void**)&p.core, words * 8, st), "core allocation");
+    CU(pool_alloc((void**)&p.core, words * 8, st, kPoolCore), "core allocation");
     m->device_bytes += words * 8;
     CU(launch_core_build(m->desc, m->arena, want, p.core, st), "core build");
     p.core_k = want;
   }
   if (want_fw) {
     const uint64_t fwords = (uint64_t)(want_fk - kFilterLo) * want_fw;
-    CU(pool_alloc((void**)&p.filter, fwords * 8, st), "row filter allocation");
+    CU(pool_alloc((void**)&p.filter, fwords * 8, st, kPoolCore), "row filter allocation");
     m->device_bytes += fwords * 8;
     CU(launch_filter_build(m->desc, m->arena, want_fk, want_fw, p.filter, st), "row filter build");
     p.filter_words = want_fw;

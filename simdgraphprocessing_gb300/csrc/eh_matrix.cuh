@@ -84,15 +84,21 @@ struct Matrix {
 
 // eh_capi.cu
 // Stream-ordered allocation (cudaMallocAsync semantics) from the library's own
-// pool on the current device, for scratch and for a matrix's buffers, all freed
+// pools on the current device, for scratch and for a matrix's buffers, all freed
 // with cudaFreeAsync: scratch on the stream that used it, a matrix's buffers on
 // a stream made to wait for the matrix's recorded uses (note_use / wait_uses).
-// The pool keeps up to kPoolKeep bytes of freed memory mapped between calls:
+// Each pool keeps up to kPoolKeep bytes of freed memory mapped between calls:
 // the device's default pool releases it at every synchronisation, and mapping
 // 400 MB again costs about 1 ms on GB300.  16 GiB holds a rebuilt scale-22
 // matrix with its largest tuned core (4.3 GB) and its build scratch.
 constexpr uint64_t kPoolKeep = 16ull << 30;
-cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st);
+// Which pool: the dense cores and row filters of work plans (large, and kept
+// for the matrix's life) come from a pool of their own.  In the same pool as
+// the other buffers, a resident 4.3 GB core made every later build and plan
+// of another matrix 0.6 + 0.6 ms slower at scale 22; in their own pool (or
+// from cudaMalloc) it costs nothing.
+enum PoolKind { kPoolMain = 0, kPoolCore = 1 };
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st, PoolKind kind = kPoolMain);
 // A non-blocking stream of the current device for host uploads that overlap
 // the build (one per device, created on first use).
 cudaError_t upload_stream(cudaStream_t* out);
