@@ -442,7 +442,7 @@ def run_ours(a, rank, world, local_rank):
                "; C oracle port of the reference algorithm (OpenMP, build %.2f s untimed)" % tb,
                "count_matches_gpu": (ccount == count) if ccount is not None else None}
     # Roofline: the physical HBM figure is the count's DRAM traffic (ncu, the
-    # two pivot kernels of one count) over the event-timed count.  The survey's
+    # two pivot kernels of one count) over the event-timed count.  The
     # algorithmic bytes B_tc charge every neighbour row in full per edge while
     # the kernels probe words of it (much of it from L2), so B_tc / time is an
     # effective bandwidth above what HBM can deliver, reported beside it.
