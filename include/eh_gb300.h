@@ -281,7 +281,8 @@ eh_status eh_bfs_path_length(eh_matrix_t m, uint32_t start, uint64_t max_depth, 
 /* Work-shape autotuning (no reference counterpart).                           */
 /* ------------------------------------------------------------------------- */
 typedef struct eh_tuning {
-  uint32_t light_max;     /* pivots with at most this many entries run one per warp */
+  uint32_t light_max;     /* pivots with at most this many entries (2..160) run one
+                             per warp                                               */
   uint32_t unit_span;     /* pivot positions per CTA work unit for larger pivots    */
   uint32_t ctas_per_sm;   /* resident CTAs per SM of the persistent count kernel     */
   uint32_t core_rows;     /* highest-degree rows kept as a dense bitmap (0 = none)   */
@@ -311,10 +312,13 @@ eh_status eh_matrix_tune(eh_matrix_t m, void* stream, eh_tuning* result);
  * reference counterpart.) */
 eh_status eh_matrix_tune_for(eh_matrix_t m, uint32_t counts_per_build, void* stream, eh_tuning* result);
 /* Uses the given work shape (light_max, unit_span, ctas_per_sm, core_rows,
- * core_hot_words, core_filter_words of `shape`; ms and configs_tried are ignored) for this
- * matrix's later counts, rebuilding its plan as needed; a cached tuned shape no
- * longer applies to this matrix.  Counts do not depend on the shape.  EH_ERR_INVALID_ARGUMENT for a value outside the tuner's
- * ranges.  (No reference counterpart.) */
+ * core_hot_words, core_filter_words of `shape`; ms and configs_tried are
+ * ignored) for this matrix's later counts, rebuilding its plan as needed; a
+ * cached tuned shape no longer applies to this matrix.  Counts do not depend
+ * on the shape.  EH_ERR_INVALID_ARGUMENT for a value outside the tuner's
+ * ranges (light_max 2..160, unit_span 1..65536, ctas_per_sm 1..the kernel's
+ * occupancy, core_rows <= 262,144, core_filter_words 0/16/32/64).  (No
+ * reference counterpart.) */
 eh_status eh_matrix_set_shape(eh_matrix_t m, const eh_tuning* shape, void* stream);
 
 /* ------------------------------------------------------------------------- */
