@@ -252,6 +252,17 @@ eh_status eh_similar_nodes_async(eh_matrix_t m, uint32_t threshold, uint64_t* d_
  * with EH_SELECT_LOWER. */
 eh_status eh_list_triangles(eh_matrix_t m, uint32_t* d_out, uint64_t capacity, uint64_t* d_total,
                             void* stream);
+/* Clique tuples, as n_clique<T,R> writes them with WRITE_TABLE
+ * (apps/n_clique.cpp:30-50: at the last level Table<T>::write_table appends one
+ * tuple per element of C, src/Table.hpp:30-43): every k-clique (x_1, ..., x_k)
+ * with x_1 > x_2 > ... > x_k, x_1 the pivot row and the others entries of
+ * row(x_1) in descending order, written as k u32 row ids to
+ * d_out[k*t .. k*t+k-1] for t < capacity, in no particular order; *d_total
+ * (device) receives the number of cliques, which equals eh_count_cliques(m, k)
+ * (tuples past capacity are counted, not written).  k = 3 or 4
+ * (EH_ERR_UNSUPPORTED otherwise).  Matrix built with EH_SELECT_LOWER. */
+eh_status eh_list_cliques(eh_matrix_t m, uint32_t k, uint32_t* d_out, uint64_t capacity, uint64_t* d_total,
+                          void* stream);
 /* ops::set_intersect on rows (src/set/ops/intersection.hpp, dispatcher :2067-2117):
  * d_counts[p] = |row(d_a[p]) ∩ row(d_b[p])| for p < npairs (device arrays);
  * a pair that names a row >= matrix_size gets 0xffffffff. */

@@ -814,6 +814,62 @@ uint64_t oracle_dump(void* mp, uint8_t* buf) {
   return pos;
 }
 
+/* n_clique<T,R>::apply_function with WRITE_TABLE (apps/n_clique.cpp:30-50):
+ * the tuple holds the pivot and one element per level; at the last level
+ * Table<T>::write_table (src/Table.hpp:30-43) appends one tuple per element
+ * of C.  Writes up to cap tuples of k u32 in the reference's loop order. */
+static void list_function(const omatrix* m, uint64_t node, uint64_t depth, uint64_t k, oset* sets,
+                          clique_scratch* s, uint32_t* tuple, uint32_t* out, uint64_t cap, uint64_t* total) {
+  oset C;
+  set_intersect(sets[depth - 1], get_row(m, node), s->bufs[depth], &C);
+  sets[depth] = C;
+  tuple[depth - 1] = (uint32_t)node;
+  ++depth;
+  uint64_t ne = decode(C, s->elems[depth]);
+  for (uint64_t e = 0; e < ne; e++) {
+    if (depth == k) {
+      if (*total < cap) {
+        for (uint64_t d = 0; d + 1 < k; d++) out[k * *total + d] = tuple[d];
+        out[k * *total + k - 1] = s->elems[depth][e];
+      }
+      (*total)++;
+    } else {
+      list_function(m, s->elems[depth][e], depth, k, sets, s, tuple, out, cap, total);
+    }
+  }
+}
+/* n_clique<T,R>::run with WRITE_TABLE (apps/n_clique.cpp:52-101), one thread,
+ * 3 <= k <= 16; returns the number of cliques. */
+uint64_t oracle_list_cliques(void* mp, int k, uint32_t* out, uint64_t cap) {
+  omatrix* m = (omatrix*)mp;
+  if (k < 3 || k > 16) return 0;
+  uint64_t maxc = 1, maxb = 16, total = 0;
+  for (uint64_t i = 0; i < m->n; i++) {
+    if (m->row_lengths[i] > maxc) maxc = m->row_lengths[i];
+    if (m->row_offsets[i + 1] - m->row_offsets[i] > maxb) maxb = m->row_offsets[i + 1] - m->row_offsets[i];
+  }
+  uint64_t bufsz = (maxb > maxc * 4 ? maxb : maxc * 4) + 64;
+  clique_scratch s;
+  s.bufs = (uint8_t**)malloc((k + 1) * sizeof(uint8_t*));
+  s.elems = (uint32_t**)malloc((k + 1) * sizeof(uint32_t*));
+  for (int d = 0; d <= k; d++) {
+    s.bufs[d] = (uint8_t*)malloc(bufsz);
+    s.elems[d] = (uint32_t*)malloc((maxc + 16) * 4);
+  }
+  oset* sets = (oset*)malloc((k + 1) * sizeof(oset));
+  uint32_t tuple[16];
+  for (uint64_t i = 0; i < m->n; i++) {
+    oset A = get_row(m, i);
+    sets[1] = A;
+    tuple[0] = (uint32_t)i;
+    uint64_t ne = decode(A, s.elems[1]);
+    for (uint64_t e = 0; e < ne; e++) list_function(m, s.elems[1][e], 2, (uint64_t)k, sets, &s, tuple, out, cap, &total);
+  }
+  for (int d = 0; d <= k; d++) { free(s.bufs[d]); free(s.elems[d]); }
+  free(s.bufs); free(s.elems); free(sets);
+  return total;
+}
+
 /* Triangle tuples as undirected_triangle_counting would emit them with tuple
  * output on (Table<T>::write_table, src/Table.hpp:30-43): for every pivot i and
  * j in row(i), each k in row(i) ∩ row(j) gives (i, j, k).  Writes up to cap

@@ -71,6 +71,8 @@ def lib():
         L.oracle_n_path.argtypes = [P, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint64)]
         L.oracle_list_triangles.restype = C.c_uint64
         L.oracle_list_triangles.argtypes = [P, P, C.c_uint64]
+        L.oracle_list_cliques.restype = C.c_uint64
+        L.oracle_list_cliques.argtypes = [P, C.c_int, P, C.c_uint64]
         L.oracle_rmat.restype = C.c_uint64
         L.oracle_rmat.argtypes = [C.c_uint32, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64,
                                   C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
@@ -137,6 +139,13 @@ class Matrix:
         total = lib().oracle_list_triangles(self.h, None, 0)
         out = np.zeros((max(total, 1), 3), np.uint32)
         lib().oracle_list_triangles(self.h, _ptr(out), total)
+        return out[:total]
+
+    def list_cliques(self, k=4):
+        """(Q, k) u32 array of k-clique tuples, descending ids, in the reference's loop order."""
+        total = lib().oracle_list_cliques(self.h, k, None, 0)
+        out = np.zeros((max(total, 1), k), np.uint32)
+        lib().oracle_list_cliques(self.h, k, _ptr(out), total)
         return out[:total]
 
     def triangles_range(self, lo, hi):

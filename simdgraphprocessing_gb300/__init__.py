@@ -129,6 +129,7 @@ def load(build_if_missing=True):
         "eh_bfs_path_length": (I, [P, U32, U64, C.POINTER(U64), C.POINTER(U64), P]),
         "eh_selftest_bounded_wait": (I, [U32, C.POINTER(U32)]),
         "eh_list_triangles": (I, [P, P, U64, P, P]),
+        "eh_list_cliques": (I, [P, U32, P, U64, P, P]),
         "eh_matrix_tune": (I, [P, P, C.POINTER(Tuning)]),
         "eh_matrix_tune_for": (I, [P, C.c_uint32, P, C.POINTER(Tuning)]),
         "eh_matrix_set_shape": (I, [P, C.POINTER(Tuning), P]),
@@ -437,6 +438,11 @@ class Matrix:
     def list_triangles(self, d_out, capacity, d_total, stream=None):
         check(load().eh_list_triangles(self.h, C.c_void_p(d_out), capacity, C.c_void_p(d_total),
                                        _stream(stream)))
+
+    def list_cliques(self, k, d_out, capacity, d_total, stream=None):
+        """eh_list_cliques: k-clique tuples (k = 3 or 4) into device memory."""
+        check(load().eh_list_cliques(self.h, k, C.c_void_p(d_out), capacity, C.c_void_p(d_total),
+                                     _stream(stream)))
 
     def tune(self, stream=None, counts_per_build=0):
         """eh_matrix_tune, or eh_matrix_tune_for when counts_per_build > 0."""

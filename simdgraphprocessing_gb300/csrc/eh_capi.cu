@@ -464,7 +464,8 @@ static eh_status finish_sync(Matrix* m, unsigned long long* d_res, uint64_t* cou
 }
 
 eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const uint32_t* graph_rows,
-                         uint32_t num_graphs, cudaStream_t st, Workspace* ws) {
+                         uint32_t num_graphs, cudaStream_t st, Workspace* ws, bool list, uint32_t* tuples,
+                         uint64_t capacity) {
   Workspace own;
   if (!ws) {
     own.counters = m->counters;
@@ -490,7 +491,7 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
   const uint32_t nG = p.above(cap);
   const uint32_t nB = p.above(32);
   const uint32_t nL = p.above(k - 2);
-  CliqueArgs a{m->desc, m->arena, p.order, k, out, graph_rows, num_graphs, p.core, p.core_k};
+  CliqueArgs a{m->desc, m->arena, p.order, k, out, graph_rows, num_graphs, p.core, p.core_k, tuples, capacity};
   CU(cudaMemsetAsync(w.counters, 0, 16 * sizeof(uint32_t), st), "memset");
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
@@ -515,7 +516,7 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
         w.clique_scratch_words = m->clique_scratch_words;
       }
     }
-    CU(launch_clique_cta(a, 0, nG, w.counters + 2, cmax, w.clique_scratch, grid, st), "clique kernel (global)");
+    CU(launch_clique_cta(a, 0, nG, w.counters + 2, cmax, w.clique_scratch, grid, st, list), "clique kernel (global)");
   }
   // The shared-memory tier runs in size bands, each launch sized for its own
   // largest pivot, so that the many small pivots are not held to the
@@ -528,11 +529,11 @@ eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const u
     const uint32_t p0 = p.above(bands[b]), p1 = p.above(bands[b + 1]);
     if (p1 <= p0) continue;
     const uint32_t cmax = p.largest_at_most(bands[b]);
-    CU(launch_clique_cta(a, p0, p1, w.counters + 3 + b, cmax, nullptr, 0, st), "clique kernel (shared)");
+    CU(launch_clique_cta(a, p0, p1, w.counters + 3 + b, cmax, nullptr, 0, st, list), "clique kernel (shared)");
   }
   if (nL > nB) {
     const int grid = (int)std::min<uint64_t>((nL - nB + 63) / 64, 8ull * sms);
-    CU(launch_clique_light(a, nB, nL, w.counters + 11, grid > 0 ? grid : 1, st), "clique kernel (warp)");
+    CU(launch_clique_light(a, nB, nL, w.counters + 11, grid > 0 ? grid : 1, st, list), "clique kernel (warp)");
   }
   note_use(m, st);
   return EH_OK;
@@ -873,6 +874,16 @@ eh_status eh_count_cliques_async(eh_matrix_t mh, uint32_t k, uint64_t* d_count, 
   CHECK_MATRIX(mh);
   EH_CHECK_ARG(d_count, "d_count is NULL");
   return eh::launch_cliques(MX(mh), k, reinterpret_cast<unsigned long long*>(d_count), nullptr, 0, ST(stream));
+}
+
+eh_status eh_list_cliques(eh_matrix_t mh, uint32_t k, uint32_t* d_out, uint64_t capacity, uint64_t* d_total,
+                          void* stream) {
+  CHECK_MATRIX(mh);
+  EH_CHECK_ARG(d_total, "d_total is NULL");
+  EH_CHECK_ARG(capacity == 0 || d_out, "d_out is NULL");
+  if (k != 3 && k != 4) return set_error(EH_ERR_UNSUPPORTED, "clique tuples are written for k = 3 or 4, not %u", k);
+  return eh::launch_cliques(MX(mh), k, reinterpret_cast<unsigned long long*>(d_total), nullptr, 0, ST(stream),
+                            nullptr, true, d_out, capacity);
 }
 
 eh_status eh_count_cliques(eh_matrix_t mh, uint32_t k, uint64_t* count, void* stream) {

@@ -52,7 +52,22 @@ __host__ __device__ __forceinline__ uint32_t mask_off(uint32_t e) {
   return 1 + 32 * (A * (A + 1) / 2 + A / 2) + r * ((A + 1) | 1);
 }
 
+// Tuple output: the k ids of one clique (pivot row, then pivot entries in
+// descending order) at the position the cursor a.out[0] hands out, if it is
+// below the capacity.
+__device__ __forceinline__ void put_tuple(const CliqueArgs& a, unsigned long long pos, uint32_t row, uint32_t x1,
+                                          uint32_t x2, uint32_t x3) {
+  if (pos >= a.capacity) return;
+  uint32_t* o = a.tuples + pos * a.k;
+  o[0] = row;
+  o[1] = x1;
+  o[2] = x2;
+  if (a.k == 4) o[3] = x3;
+}
+
 // ---- light tier: |A_i| <= 32, one warp per pivot, one-word masks ----
+// LIST: write the k = 3 or 4 cliques as tuples instead of counting them.
+template <bool LIST>
 __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint32_t pos_begin,
                                                               uint32_t pos_end, uint32_t* counter) {
   __shared__ uint32_t s_list[NW][32];
@@ -94,6 +109,32 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
         while (t >= e && e < c) { t -= e; e++; }
       }
       __syncwarp();
+      if (LIST) {
+        // Lane e lists the cliques whose two largest members are i and A_i[e]:
+        // (i, A_i[e], A_i[t]) for t in M[e], or (i, A_i[e], A_i[t], A_i[u]) for
+        // u in M[e] & M[t]; one cursor atomic per warp and pivot.
+        const uint32_t m0 = lane < c ? mask[lane] : 0u;
+        uint32_t n = 0;
+        if (top == 0) {
+          n = __popc(m0);
+        } else {
+          for (uint32_t m = m0; m; m &= m - 1) n += __popc(m0 & mask[__ffs(m) - 1]);
+        }
+        const uint32_t ex = warp_exclusive_scan(n, lane);
+        unsigned long long base = 0;
+        if (lane == 31 && ex + n) base = atomicAdd(a.out, (unsigned long long)(ex + n));
+        base = __shfl_sync(FULL, base, 31) + ex;
+        for (uint32_t m = base < a.capacity ? m0 : 0u; m; m &= m - 1) {  // past the capacity: counted only
+          const uint32_t tt = __ffs(m) - 1;
+          if (top == 0) {
+            put_tuple(a, base++, row, list[lane], list[tt], 0u);
+          } else {
+            for (uint32_t r = m0 & mask[tt]; r; r &= r - 1) put_tuple(a, base++, row, list[lane], list[tt], list[__ffs(r) - 1]);
+          }
+        }
+        __syncwarp();
+        continue;
+      }
       // phase 2: lane e counts the cliques whose two largest members are i and A_i[e]
       if (lane < c) {
         const uint32_t m0 = mask[lane];
@@ -139,7 +180,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
     }
   }
   acc = warp_sum_u64(acc);
-  if (lane == 0 && acc) atomicAdd(a.out, acc);
+  if (!LIST && lane == 0 && acc) atomicAdd(a.out, acc);
 }
 
 // ---- CTA tiers: one pivot per CTA; masks in shared memory or a global slot ----
@@ -147,7 +188,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_clique_light(CliqueArgs a, uint
 // (stacks only for k >= 5); W = mask_len(cmax) is the DFS stack row length.
 // NT threads per CTA: 256, or 1,024 for the largest pivots at k <= 4, whose
 // masks leave room for one CTA per SM (more warps to hide latency).
-template <bool GLOBAL, int NT>
+template <bool GLOBAL, int NT, bool LIST>
 __global__ void __launch_bounds__(NT, NT == 1024 ? 1 : (GLOBAL ? 2 : 8)) k_clique_cta(CliqueArgs a, uint32_t pos_begin, uint32_t pos_end,
                                                             uint32_t* counter, uint32_t cmax, uint32_t W,
                                                             uint32_t* gscratch, uint64_t slot_words) {
@@ -213,6 +254,41 @@ __global__ void __launch_bounds__(NT, NT == 1024 ? 1 : (GLOBAL ? 2 : 8)) k_cliqu
     for (uint32_t e = 1 + warp; e < c; e += NW) {
       const uint32_t* Me = masks + mask_off(e);
       const uint32_t we = (e + 31) >> 5;  // words that can hold bits < e
+      if (LIST) {
+        // Lane t of each word of M[e] lists (i, A_i[e], A_i[t]) or, for k = 4,
+        // (i, A_i[e], A_i[t], A_i[u]) for u in M[e] & M[t], one cursor atomic per word of M[e].
+        // Tuples past the capacity are counted, not enumerated.
+        const uint32_t je = list[e];
+        for (uint32_t w = 0; w < we; w++) {
+          const uint32_t bits = Me[w];
+          if (top == 0) {  // one cursor atomic per word of M[e]
+            if (!bits) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(a.out, (unsigned long long)__popc(bits));
+            base = __shfl_sync(FULL, base, 0);
+            if ((bits >> lane) & 1u)
+              put_tuple(a, base + __popc(bits & ((1u << lane) - 1u)), row, je, list[32 * w + lane], 0u);
+            continue;
+          }
+          if (!bits) continue;  // k = 4: lane t of the word counts M[e] & M[t], one cursor atomic per word
+          const bool has = (bits >> lane) & 1u;
+          const uint32_t t = 32 * w + lane;
+          const uint32_t* Mt = masks + mask_off(t);
+          const uint32_t lt = (t + 31) >> 5;
+          uint32_t n = 0;
+          if (has)
+            for (uint32_t x = 0; x < lt; x++) n += __popc(Me[x] & Mt[x]);
+          const uint32_t ex = warp_exclusive_scan(n, lane);
+          const uint32_t sum = __shfl_sync(FULL, ex + n, 31);
+          unsigned long long pos = 0;
+          if (lane == 0 && sum) pos = atomicAdd(a.out, (unsigned long long)sum);
+          pos = __shfl_sync(FULL, pos, 0) + ex;
+          if (has)
+            for (uint32_t x = 0; x < lt && pos < a.capacity; x++)
+              for (uint32_t r = Me[x] & Mt[x]; r; r &= r - 1) put_tuple(a, pos++, row, je, list[t], list[32 * x + __ffs(r) - 1]);
+        }
+        continue;
+      }
       if (top == 0) {
         for (uint32_t w = lane; w < we; w += 32) acc += __popc(Me[w]);
       } else if (top == 1) {
@@ -302,7 +378,7 @@ __global__ void __launch_bounds__(NT, NT == 1024 ? 1 : (GLOBAL ? 2 : 8)) k_cliqu
     __syncthreads();
   }
   acc = warp_sum_u64(acc);
-  if (lane == 0 && acc) atomicAdd(a.out, acc);
+  if (!LIST && lane == 0 && acc) atomicAdd(a.out, acc);
 }
 
 }  // namespace
@@ -335,7 +411,7 @@ uint32_t clique_smem_cap(uint32_t k, int device) {
 // SMs x resident CTAs of the shared-memory clique kernel with `bytes` of
 // dynamic shared memory; looked up once per (device, size), so that launches
 // captured into a CUDA graph after a direct run make no occupancy query.
-template <int NT>
+template <int NT, bool LIST>
 static int resident_ctas(int dev, size_t bytes) {
   static std::mutex mu;
   static std::map<std::pair<int, size_t>, int> cache;
@@ -344,14 +420,14 @@ static int resident_ctas(int dev, size_t bytes) {
   if (it != cache.end()) return it->second;
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clique_cta<false, NT>, NT, bytes);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_clique_cta<false, NT, LIST>, NT, bytes);
   const int g = std::max(sms, 1) * std::max(per, 1);
   cache[{dev, bytes}] = g;
   return g;
 }
 
 // Shared-memory launch with NT threads per CTA.
-template <int NT>
+template <int NT, bool LIST>
 static cudaError_t launch_shared(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                                  uint32_t cmax, uint32_t W, uint64_t slot, int grid, cudaStream_t st) {
   const size_t bytes = slot * 4;
@@ -362,7 +438,7 @@ static cudaError_t launch_shared(const CliqueArgs& a, uint32_t pos_begin, uint32
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if ((int)bytes > set_bytes[dev].load()) {
-    cudaError_t e = cudaFuncSetAttribute(k_clique_cta<false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_clique_cta<false, NT, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)bytes);
     if (e != cudaSuccess) return e;
     int prev = set_bytes[dev].load();
@@ -370,21 +446,22 @@ static cudaError_t launch_shared(const CliqueArgs& a, uint32_t pos_begin, uint32
     }
   }
   if (grid <= 0)  // fill the GPU: SMs x resident CTAs at this shared-memory size, at most one per pivot
-    grid = (int)std::min<uint64_t>(pos_end - pos_begin, (uint64_t)resident_ctas<NT>(dev, bytes));
-  k_clique_cta<false, NT><<<grid, NT, bytes, st>>>(a, pos_begin, pos_end, counter, cmax, W, nullptr, slot);
+    grid = (int)std::min<uint64_t>(pos_end - pos_begin, (uint64_t)resident_ctas<NT, LIST>(dev, bytes));
+  k_clique_cta<false, NT, LIST><<<grid, NT, bytes, st>>>(a, pos_begin, pos_end, counter, cmax, W, nullptr, slot);
   return cudaGetLastError();
 }
 
 cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
-                                int grid, cudaStream_t st) {
+                                int grid, cudaStream_t st, bool list) {
   if (pos_end <= pos_begin) return cudaSuccess;
-  k_clique_light<<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter);
+  if (list) k_clique_light<true><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter);
+  else k_clique_light<false><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter);
   return cudaGetLastError();
 }
 
-cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
+template <bool LIST>
+static cudaError_t launch_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
                               uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st) {
-  if (pos_end <= pos_begin) return cudaSuccess;
   const uint32_t W = mask_len(cmax);
   const uint64_t slot = clique_slot_words(cmax, a.k);
   const bool wide = a.k <= 4 && cmax > kCliqueWideMin;
@@ -395,15 +472,23 @@ cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t 
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       grid = std::max(1, std::min(grid, sms));
-      k_clique_cta<true, 1024><<<grid, 1024, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch, slot);
+      k_clique_cta<true, 1024, LIST><<<grid, 1024, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W, gscratch,
+                                                            slot);
     } else {
-      k_clique_cta<true, kCtaThreads><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W,
-                                                                    gscratch, slot);
+      k_clique_cta<true, kCtaThreads, LIST><<<grid, kCtaThreads, 0, st>>>(a, pos_begin, pos_end, counter, cmax, W,
+                                                                          gscratch, slot);
     }
     return cudaGetLastError();
   }
-  return wide ? launch_shared<1024>(a, pos_begin, pos_end, counter, cmax, W, slot, grid, st)
-              : launch_shared<kCtaThreads>(a, pos_begin, pos_end, counter, cmax, W, slot, grid, st);
+  return wide ? launch_shared<1024, LIST>(a, pos_begin, pos_end, counter, cmax, W, slot, grid, st)
+              : launch_shared<kCtaThreads, LIST>(a, pos_begin, pos_end, counter, cmax, W, slot, grid, st);
+}
+
+cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
+                              uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st, bool list) {
+  if (pos_end <= pos_begin) return cudaSuccess;
+  return list ? launch_cta<true>(a, pos_begin, pos_end, counter, cmax, gscratch, grid, st)
+              : launch_cta<false>(a, pos_begin, pos_end, counter, cmax, gscratch, grid, st);
 }
 
 }  // namespace eh

@@ -160,6 +160,11 @@ struct CliqueArgs {
   uint32_t num_graphs;
   const unsigned long long* core;  // dense core bitmap (rows j < core_k), or null
   uint32_t core_k;
+  // Tuple output (the list kernels, k = 3 or 4): clique j of the count goes to
+  // tuples[k*j .. k*j+k-1] when j < capacity; out[0] is the count and the
+  // cursor that hands out j.
+  uint32_t* tuples;
+  uint64_t capacity;
 };
 constexpr uint32_t kCliqueMaxK = 16;
 // Largest pivot row a clique count accepts: a pivot's packed masks are indexed
@@ -170,7 +175,7 @@ constexpr uint32_t kCliqueSmemMax = 2048;  // no pivot above this size keeps its
 // Words of one pivot's working set (list, masks, per-warp DFS stacks).
 uint64_t clique_slot_words(uint32_t cmax, uint32_t k);
 cudaError_t launch_clique_light(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
-                                int grid, cudaStream_t st);
+                                int grid, cudaStream_t st, bool list = false);
 // Largest pivot (<= kCliqueSmemMax) whose k-clique working set fits one CTA's
 // opt-in shared memory on `device`; larger pivots use global scratch slots.
 uint32_t clique_smem_cap(uint32_t k, int device);
@@ -178,6 +183,6 @@ uint32_t clique_smem_cap(uint32_t k, int device);
 // as fit on the GPU, at most one per pivot); else grid slots of
 // clique_slot_words(cmax, k) words each in global memory.
 cudaError_t launch_clique_cta(const CliqueArgs& a, uint32_t pos_begin, uint32_t pos_end, uint32_t* counter,
-                              uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st);
+                              uint32_t cmax, uint32_t* gscratch, int grid, cudaStream_t st, bool list = false);
 
 }  // namespace eh

@@ -136,7 +136,9 @@ PivotArgs pivot_args(Matrix* m, unsigned long long* out);
 eh_status launch_triangle_count(Matrix* m, unsigned long long* out, const uint32_t* graph_rows, uint32_t num_graphs,
                                 cudaStream_t st, Workspace* ws = nullptr);
 eh_status launch_lollipop_count(Matrix* m, unsigned long long* out, cudaStream_t st);
+// tuples != null or list: write the k = 3 or 4 cliques as tuples (CliqueArgs::tuples).
 eh_status launch_cliques(Matrix* m, uint32_t k, unsigned long long* out, const uint32_t* graph_rows,
-                         uint32_t num_graphs, cudaStream_t st, Workspace* ws = nullptr);
+                         uint32_t num_graphs, cudaStream_t st, Workspace* ws = nullptr, bool list = false,
+                         uint32_t* tuples = nullptr, uint64_t capacity = 0);
 
 }  // namespace eh
