@@ -47,3 +47,19 @@ def test_three_tier_mode_agrees(eh, oracle):
     spec = _golden.graphs()[5]
     off, nbr = _golden.generate(eh, spec)
     assert oracle.counts(off, nbr, "hybrid3") == spec["counts"]["hybrid"]
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_oracle_clique_tables_match_counts(oracle, layout, tmp_path):
+    """The oracle's n_clique table output (WRITE_TABLE) on the reference's
+    facebook graph: as many 4-clique tuples as the gtest golden count, each
+    descending; the 3-clique table is the triangle table."""
+    import numpy as np
+    off, nbr, _ = oracle.read_binary(_golden.fixture_graph("facebook.bin", tmp_path))
+    m = oracle.Matrix(off, nbr, oracle.SELECT_LOWER, oracle.LAYOUTS[layout])
+    t4 = m.list_cliques(4)
+    assert len(t4) == _golden.load()["reference_gtest_goldens"]["cliques4"]
+    assert all(np.all(t4[:, d] > t4[:, d + 1]) for d in range(3))
+    t3 = m.list_cliques(3)
+    tt = m.list_triangles()
+    assert np.array_equal(t3, tt)
