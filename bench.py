@@ -56,7 +56,7 @@ def parse_args():
                         "--scale 16 --edges 1000000 --seed 1 --layout uint)")
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--layout", default="hybrid")
-    p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile", action="store_true", help="minimal run for ncu captures")
