@@ -36,6 +36,7 @@ namespace {
 
 constexpr int NWARPS = kCtaThreads / 32;
 constexpr uint32_t kLightChunk = 16;  // light pivots per atomic grab
+constexpr uint32_t kTinyPairs = 28;   // chunks of pivots with at most this many pairs (8 entries) share steps
 constexpr uint32_t kStreamMinE = 256;  // core rows: consider streaming row(j) only past this many probes
 
 struct __align__(16) HeavySmem {
@@ -249,12 +250,93 @@ __device__ __forceinline__ unsigned long long core_word(const PivotArgs& a, uint
   return (x >> 6) < a.core_hot_words ? ld_keep(p) : ld_stream(p);
 }
 
+// Two light-pivot probes at once, x0 in row(j0) and (if two) x1 in row(j1):
+// the row's filter word first (if the row has a filter; a clear bit means x is
+// not in row(j)), then one word of the core row j when j < core_k, else the
+// row itself.  Both probes' loads are issued before either result is used.
+// Returns the hits as bits 0 and 1.
+template <bool HOT>
+__device__ __forceinline__ uint32_t probe2(const PivotArgs& a, uint32_t j0, uint32_t x0, uint32_t j1, uint32_t x1,
+                                           bool two) {
+  const uint32_t b0 = filter_bit(x0, a.filter_words), b1 = filter_bit(x1, a.filter_words);
+  const unsigned long long f0 = (j0 >= kFilterLo && j0 < a.filter_k)
+                                    ? ld_keep(a.filter + (uint64_t)(j0 - kFilterLo) * a.filter_words + (b0 >> 6))
+                                    : ~0ull;
+  const unsigned long long f1 = (two && j1 >= kFilterLo && j1 < a.filter_k)
+                                    ? ld_keep(a.filter + (uint64_t)(j1 - kFilterLo) * a.filter_words + (b1 >> 6))
+                                    : ~0ull;
+  const bool m0 = (f0 >> (b0 & 63)) & 1ull, m1 = two && ((f1 >> (b1 & 63)) & 1ull);
+  const bool c0 = m0 && j0 < a.core_k, c1 = m1 && j1 < a.core_k;
+  const unsigned long long v0 = c0 ? core_word<HOT>(a, j0, x0) : 0ull;
+  const unsigned long long v1 = c1 ? core_word<HOT>(a, j1, x1) : 0ull;
+  uint32_t h0 = (uint32_t)((v0 >> (x0 & 63)) & 1ull), h1 = (uint32_t)((v1 >> (x1 & 63)) & 1ull);
+  if (m0 && !c0) h0 = row_contains(load_view(a.desc, a.arena, j0), x0);
+  if (m1 && !c1) h1 = row_contains(load_view(a.desc, a.arena, j1), x1);
+  return h0 | (h1 << 1);
+}
+
+// A chunk of light pivots whose first (largest) pivot has at most kTinyPairs
+// pairs, as one pair space: the pivots' descriptors and rows are loaded by one
+// lane each, and lane q of a step takes pair q of the whole chunk, so a pivot
+// of a few pairs does not hold the warp for a step of its own.  Out of line:
+// its registers do not weigh on the main loop.  Returns the chunk's count
+// (each hit weighted by its pivot's card for lollipops).
+template <bool LOLLI, bool HOT>
+__device__ __noinline__ unsigned long long light_tiny_chunk(const PivotArgs& a, uint32_t base, uint32_t end,
+                                                            uint32_t* list, uint32_t* pstart, uint32_t* poff,
+                                                            uint32_t* pcard, uint32_t lane) {
+  const uint32_t g = end - base;  // <= kLightChunk <= 32
+  RowView V;
+  uint32_t cl = 0;
+  if (lane < g) {
+    V = load_view(a.desc, a.arena, a.order[a.n_heavy + base + lane]);
+    cl = V.card;  // <= the first pivot's card: rows in descending card order
+  }
+  const uint32_t pl = cl * (cl - 1) / 2;
+  const uint32_t off = warp_exclusive_scan(cl, lane), pex = warp_exclusive_scan(pl, lane);
+  const uint32_t total = __shfl_sync(FULL, pex + pl, 31);
+  if (lane < g) {
+    pstart[lane] = pex;
+    poff[lane] = off;
+    pcard[lane] = cl;
+  }
+  if (lane == 0) pstart[g] = total;
+  if (lane < g && V.type == TY_UINT)
+    for (uint32_t u = 0; u < cl; u++) list[off + u] = static_cast<const uint32_t*>(V.p)[u];
+  __syncwarp();
+  for (uint32_t rest = __ballot_sync(FULL, lane < g && V.type != TY_UINT); rest; rest &= rest - 1) {
+    const uint32_t p = __ffs(rest) - 1;
+    warp_decode(load_view(a.desc, a.arena, a.order[a.n_heavy + base + p]), list + poff[p], lane);
+  }
+  unsigned long long tcnt = 0;
+  for (uint32_t q = lane; q < total; q += 64) {
+    const bool two = q + 32 < total;
+    uint32_t jj[2], xx[2], ww[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const uint32_t qh = (h == 0 || two) ? q + 32u * h : q;
+      uint32_t p = 0;
+      while (pstart[p + 1] <= qh) p++;
+      uint32_t e = 1, t = qh - pstart[p];
+      while (t >= e) { t -= e; e++; }
+      jj[h] = list[poff[p] + e];
+      xx[h] = list[poff[p] + t];
+      ww[h] = LOLLI ? pcard[p] : 1u;
+    }
+    const uint32_t h = probe2<HOT>(a, jj[0], xx[0], jj[1], xx[1], two);
+    tcnt += (unsigned long long)(h & 1u) * ww[0] + (unsigned long long)(h >> 1) * ww[1];
+  }
+  __syncwarp();  // the slice and tables are reused by the next chunk
+  return tcnt;
+}
+
 // Light pivots: 8 resident CTAs per SM (64 warps, 32 registers per thread):
 // bound by the latency of scattered probes, so occupancy and two probes in
 // flight per lane pay.
 template <bool LOLLI, bool HOT>  // HOT: core_hot_words != 0
 __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
   __shared__ uint32_t wlist[NWARPS][kLightMax];
+  __shared__ uint32_t wtiny[NWARPS][3][kLightChunk + 1];  // tiny chunks: pair starts, list offsets, cards
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long acc = 0;
 
@@ -267,6 +349,15 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
     base = __shfl_sync(FULL, base, 0);
     if (base >= n_light) break;
     const uint32_t end = min(n_light, base + kLightChunk);
+    // A chunk whose first (largest) pivot has at most kTinyPairs pairs runs as
+    // one pair space: its pivots' descriptors and rows are loaded by one lane
+    // each, and lane q of a step takes pair q of the whole chunk, so a pivot
+    // of a few pairs does not hold the warp for a step of its own.
+    const RowView F = load_view(a.desc, a.arena, a.order[a.n_heavy + base]);
+    if (!a.graph_rows && F.card * (F.card - 1) / 2 <= kTinyPairs) {
+      acc += light_tiny_chunk<LOLLI, HOT>(a, base, end, list, wtiny[warp][0], wtiny[warp][1], wtiny[warp][2], lane);
+      continue;
+    }
     for (uint32_t k = base; k < end; k++) {
       const uint32_t i = a.order[a.n_heavy + k];
       const RowView A = load_view(a.desc, a.arena, i);
@@ -290,20 +381,7 @@ __global__ void __launch_bounds__(kCtaThreads, 8) k_pivots_light(PivotArgs a) {
         const uint32_t j1 = two ? list[e] : 0u, x1 = two ? list[t] : 0u;
         t += 32;
         while (t >= e && e < c) { t -= e; e++; }
-        const uint32_t b0 = filter_bit(x0, a.filter_words), b1 = filter_bit(x1, a.filter_words);
-        const unsigned long long f0 = (j0 >= kFilterLo && j0 < a.filter_k)
-                                          ? ld_keep(a.filter + (uint64_t)(j0 - kFilterLo) * a.filter_words + (b0 >> 6))
-                                          : ~0ull;
-        const unsigned long long f1 = (two && j1 >= kFilterLo && j1 < a.filter_k)
-                                          ? ld_keep(a.filter + (uint64_t)(j1 - kFilterLo) * a.filter_words + (b1 >> 6))
-                                          : ~0ull;
-        const bool m0 = (f0 >> (b0 & 63)) & 1ull, m1 = two && ((f1 >> (b1 & 63)) & 1ull);
-        const bool c0 = m0 && j0 < a.core_k, c1 = m1 && j1 < a.core_k;
-        const unsigned long long v0 = c0 ? core_word<HOT>(a, j0, x0) : 0ull;
-        const unsigned long long v1 = c1 ? core_word<HOT>(a, j1, x1) : 0ull;
-        cnt += (uint32_t)((v0 >> (x0 & 63)) & 1ull) + (uint32_t)((v1 >> (x1 & 63)) & 1ull);
-        if (m0 && !c0) cnt += row_contains(load_view(a.desc, a.arena, j0), x0);
-        if (m1 && !c1) cnt += row_contains(load_view(a.desc, a.arena, j1), x1);
+        cnt += __popc(probe2<HOT>(a, j0, x0, j1, x1, two));
       }
       unsigned long long pc = LOLLI ? (unsigned long long)cnt * c : (unsigned long long)cnt;
       if (a.graph_rows) {  // batch: one atomic per pivot into its graph's count
